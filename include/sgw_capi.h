@@ -1,0 +1,168 @@
+/*
+ * sgw_capi.h - C ABI of the GB300 Sternheimer solver (libsgw_gb300.so).
+ *
+ * Drop-in boundary for SternheimerGW's linear-solver package
+ * (algo/linear_solver).  The reference calls
+ *     select_solver(config, AA, bb, sigma, xx, ierr)      select_solver.f90:67
+ * where AA(sigma, x, Ax) applies (H + sigma S + alpha_pv P_v) through
+ * linear_op (linear_op.f90:46) using QE module state set by the caller
+ * (solve_linter.f90:315-316, green.f90:88-91).  A GPU cannot call back into a
+ * Fortran procedure, so the operator is a handle built once from that same
+ * state (G-sphere map, |k+G|^2, V_loc(r), beta, D, psi_occ, alpha_pv); the
+ * solver entry points then keep the reference's argument order and meaning.
+ *
+ * Complex values are pairs of doubles (layout of Fortran COMPLEX(dp), C99
+ * double _Complex and std::complex<double>).  Arrays are column-major with
+ * explicit leading dimensions, so Fortran array sections such as
+ * dpsi(:npwq, ibnd, :) (solve_linter.f90:368-369) pass as pointer + ldx.
+ *
+ * Errors never abort: every call returns an sgw_status; sgw_last_error()
+ * gives a one-line reason.  Status codes 0..3 mirror the reference's ierr
+ * (bicgstab.f90:249-267, linear_solver.f90:176-190), negative codes are API
+ * errors.  One CUDA stream per operator handle; a handle is not thread-safe,
+ * separate handles are independent.  No CPU fallback exists: without a usable
+ * GPU every solve returns SGW_ERR_CUDA.
+ */
+#ifndef SGW_CAPI_H
+#define SGW_CAPI_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct sgw_zcomplex {
+  double re;
+  double im;
+} sgw_zcomplex;
+
+typedef enum sgw_status {
+  SGW_OK = 0,
+  SGW_NOT_CONVERGED = 1,  /* bicgstab.f90:249-253 ierr = 1 */
+  SGW_NAN = 2,            /* bicgstab.f90:264-267 ierr = 2 */
+  SGW_BASIS_COMPLETE = 3, /* linear_solver.f90:376-378 ierr = 3 */
+  SGW_ERR_ARG = -1,
+  SGW_ERR_CUDA = -2,
+  SGW_ERR_NOMEM = -3,
+  SGW_ERR_UNSUPPORTED = -4
+} sgw_status;
+
+/* Solver codes of select_solver_type%priority (select_solver.f90:33-40). */
+enum { SGW_BICGSTAB_MULTI = 1, SGW_BICGSTAB_NO_MULTI = 2, SGW_SGW_LINEAR_SOLVER = 3 };
+
+/* select_solver_type (select_solver.f90:48-62). */
+typedef struct sgw_solver_config {
+  int32_t priority[8];  /* solver codes tried in order */
+  int32_t num_priority; /* entries of priority[] in use (reference default [1, 3]) */
+  int32_t max_iter;     /* reference default 10000 */
+  double threshold;     /* reference default 1e-4 */
+  int32_t bicg_lmax;    /* reference default 4 */
+} sgw_solver_config;
+
+/* Operator state the reference keeps in QE modules for the active k-point. */
+typedef struct sgw_pw_operator_desc {
+  int32_t npw;         /* num_g: G-vectors at k+q (ngk) */
+  int32_t npwx;        /* leading dimension of vkb/evq (>= npw) */
+  int32_t nr1, nr2, nr3; /* smooth FFT box (dffts%nr1..3) */
+  const int32_t* nl;   /* [npw] 0-based box index of each G (dffts%nl(igk_k(:))-1),
+                          box index = i1 + nr1*(i2 + nr2*i3) */
+  const double* g2kin; /* [npw] |k+q+G|^2 in Ry (g2kin) */
+  const double* vrs;   /* [nr1*nr2*nr3] local potential V(r) in Ry (vrs) */
+  int32_t nkb;         /* number of beta projectors (nkb) */
+  const sgw_zcomplex* vkb; /* [npwx x nkb] beta projectors (vkb) */
+  const double* dvan;  /* [nkb] diagonal D_ii in Ry (deeq for a diagonal D) */
+  int32_t nbnd_occ;    /* occupied bands (nbnd_occ) */
+  const sgw_zcomplex* evq; /* [npwx x nbnd_occ] occupied states at k+q (evq) */
+  double alpha_pv;     /* alpha_pv; the Green's-function operator uses 0 (green.f90:283) */
+} sgw_pw_operator_desc;
+
+typedef struct sgw_operator sgw_operator;
+
+/* Build the operator handle (device copies of all tables).  Replaces the QE
+ * module set-up done by init_us_2 / g2_kin before each solve
+ * (solve_linter.f90:315-316, green.f90:88-91). */
+sgw_status sgw_operator_create_pw(const sgw_pw_operator_desc* desc, sgw_operator** op);
+
+/* Dense operator A x + sigma x, the fake operator of the solver unit test
+ * (linear_problem.f90:100-113); a is n x n column-major with leading dim lda. */
+sgw_status sgw_operator_create_dense(int32_t n, const sgw_zcomplex* a, int64_t lda, sgw_operator** op);
+
+sgw_status sgw_operator_destroy(sgw_operator* op);
+
+/* Switch between the Coulomb operator (alpha_pv from the set-up,
+ * solve_linter.f90:657-716) and the Green's-function operator (alpha_pv = 0,
+ * green.f90:231-291) without rebuilding the handle. */
+sgw_status sgw_operator_set_alpha_pv(sgw_operator* op, double alpha_pv);
+
+/* Ax[:, i] = A(sigma) x[:, i] for m host vectors (leading dim ld); the
+ * operator AA of the reference (coulomb_operator / green_operator). */
+sgw_status sgw_operator_apply(sgw_operator* op, sgw_zcomplex sigma, int32_t m, const sgw_zcomplex* x, int64_t ldx_in,
+                              sgw_zcomplex* ax, int64_t ldx_out);
+
+/* select_solver(config, AA, bb, sigma, xx, ierr)       select_solver.f90:67-161
+ * bb[n], sigma[num_shift], xx[n x num_shift] (leading dim ldx), host memory.
+ * *ierr receives the reference's error code; the return value is *ierr or a
+ * negative API error. */
+sgw_status sgw_select_solver(sgw_operator* op, const sgw_solver_config* config, const sgw_zcomplex* bb, int32_t n,
+                             const sgw_zcomplex* sigma, int32_t num_shift, sgw_zcomplex* xx, int64_t ldx,
+                             int32_t* ierr);
+
+/* bicgstab(config, AA, bb, sigma, xx, ierr)              bicgstab.f90:154-275 */
+sgw_status sgw_bicgstab(sgw_operator* op, int32_t lmax, double threshold, int32_t max_iter, const sgw_zcomplex* bb,
+                        int32_t n, const sgw_zcomplex* sigma, int32_t num_shift, sgw_zcomplex* xx, int64_t ldx,
+                        int32_t* ierr);
+
+/* linear_solver(config, AA, bb, sigma, xx, ierr)         linear_solver.f90:82-194 */
+sgw_status sgw_linear_solver(sgw_operator* op, double threshold, int32_t max_iter, const sgw_zcomplex* bb, int32_t n,
+                             const sgw_zcomplex* sigma, int32_t num_shift, sgw_zcomplex* xx, int64_t ldx,
+                             int32_t* ierr);
+
+/* Batched multishift solve of many right-hand sides that share one operator:
+ * every (band, perturbation, frequency set) of a solve_linter call
+ * (solve_linter.f90:367-374) in one persistent launch.  Pointers are host
+ * memory (memory = 0) or device memory (memory = 1).
+ *   bb[r*ldb + g], sigma[r*lds + s], xx[r*ldr + s*ldx + g], ierr[r], iters[r].
+ * precision 0: FP64 throughout (the plain drop-in semantics).
+ * precision 1: mixed - complex64 Krylov with FP64 shift recurrences and FP64
+ *              residual refinement of the seed system (see sgw_solve_batch docs
+ *              in the package).
+ * history_iters: outer iterations kept per history window (0 = automatic). */
+typedef struct sgw_batch_desc {
+  int32_t nrhs;
+  int32_t num_shift;
+  int32_t lmax;
+  int32_t max_iter;
+  double threshold;
+  int32_t precision;
+  int32_t memory;
+  int32_t history_iters;
+  int32_t refine_max;       /* mixed: maximum FP64 refinement sweeps (0 = default 4) */
+  double refine_threshold;  /* mixed: relative FP64 seed residual target (0 = 1e-9) */
+  const sgw_zcomplex* bb;
+  int64_t ldb;
+  const sgw_zcomplex* sigma;
+  int64_t lds;
+  sgw_zcomplex* xx;
+  int64_t ldx;
+  int64_t ldr;
+  int32_t* ierr;
+  int32_t* iters;
+} sgw_batch_desc;
+
+sgw_status sgw_solve_batch(sgw_operator* op, const sgw_batch_desc* desc);
+
+/* Device time (ms) of the last solve on this handle's stream, measured with
+ * CUDA events around the kernels; and the number of kernel launches it used. */
+sgw_status sgw_last_timing(sgw_operator* op, double* ms, int64_t* launches);
+
+/* One-line description of the last error on this thread. */
+const char* sgw_last_error(void);
+
+/* Library version string. */
+const char* sgw_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SGW_CAPI_H */

@@ -1,0 +1,93 @@
+"""ctypes bindings of include/sgw_capi.h (libsgw_gb300.so, built in-tree).
+
+There is no fallback: if the shared library is missing or fails to load,
+``lib()`` raises, so nothing silently runs on the CPU.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+from . import build as _build
+
+_lib = None
+
+
+class ZComplex(C.Structure):
+    _fields_ = [("re", C.c_double), ("im", C.c_double)]
+
+
+class SolverConfig(C.Structure):
+    _fields_ = [("priority", C.c_int32 * 8), ("num_priority", C.c_int32), ("max_iter", C.c_int32),
+                ("threshold", C.c_double), ("bicg_lmax", C.c_int32)]
+
+
+class PwOperatorDesc(C.Structure):
+    _fields_ = [("npw", C.c_int32), ("npwx", C.c_int32), ("nr1", C.c_int32), ("nr2", C.c_int32), ("nr3", C.c_int32),
+                ("nl", C.c_void_p), ("g2kin", C.c_void_p), ("vrs", C.c_void_p), ("nkb", C.c_int32),
+                ("vkb", C.c_void_p), ("dvan", C.c_void_p), ("nbnd_occ", C.c_int32), ("evq", C.c_void_p),
+                ("alpha_pv", C.c_double)]
+
+
+class BatchDesc(C.Structure):
+    _fields_ = [("nrhs", C.c_int32), ("num_shift", C.c_int32), ("lmax", C.c_int32), ("max_iter", C.c_int32),
+                ("threshold", C.c_double), ("precision", C.c_int32), ("memory", C.c_int32),
+                ("history_iters", C.c_int32), ("refine_max", C.c_int32), ("refine_threshold", C.c_double),
+                ("bb", C.c_void_p), ("ldb", C.c_int64), ("sigma", C.c_void_p), ("lds", C.c_int64),
+                ("xx", C.c_void_p), ("ldx", C.c_int64), ("ldr", C.c_int64), ("ierr", C.c_void_p),
+                ("iters", C.c_void_p)]
+
+
+# (name, restype, argtypes) of every entry point declared in include/sgw_capi.h
+SIGNATURES = [
+    ("sgw_operator_create_pw", C.c_int, [C.POINTER(PwOperatorDesc), C.POINTER(C.c_void_p)]),
+    ("sgw_operator_create_dense", C.c_int, [C.c_int32, C.c_void_p, C.c_int64, C.POINTER(C.c_void_p)]),
+    ("sgw_operator_destroy", C.c_int, [C.c_void_p]),
+    ("sgw_operator_set_alpha_pv", C.c_int, [C.c_void_p, C.c_double]),
+    ("sgw_operator_apply", C.c_int, [C.c_void_p, ZComplex, C.c_int32, C.c_void_p, C.c_int64, C.c_void_p, C.c_int64]),
+    ("sgw_select_solver", C.c_int, [C.c_void_p, C.POINTER(SolverConfig), C.c_void_p, C.c_int32, C.c_void_p, C.c_int32,
+                                    C.c_void_p, C.c_int64, C.POINTER(C.c_int32)]),
+    ("sgw_bicgstab", C.c_int, [C.c_void_p, C.c_int32, C.c_double, C.c_int32, C.c_void_p, C.c_int32, C.c_void_p,
+                               C.c_int32, C.c_void_p, C.c_int64, C.POINTER(C.c_int32)]),
+    ("sgw_linear_solver", C.c_int, [C.c_void_p, C.c_double, C.c_int32, C.c_void_p, C.c_int32, C.c_void_p, C.c_int32,
+                                    C.c_void_p, C.c_int64, C.POINTER(C.c_int32)]),
+    ("sgw_solve_batch", C.c_int, [C.c_void_p, C.POINTER(BatchDesc)]),
+    ("sgw_last_timing", C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_int64)]),
+    ("sgw_last_error", C.c_char_p, []),
+    ("sgw_version", C.c_char_p, []),
+]
+
+
+def lib_path() -> str:
+    return _build.LIB
+
+
+def lib(build_if_missing: bool = True):
+    """Load libsgw_gb300.so (building it first if asked and absent)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(_build.LIB):
+            if not build_if_missing:
+                raise RuntimeError(f"{_build.LIB} is missing: run sternheimergw_gb300.build.build()")
+            _build.build()
+        L = C.CDLL(_build.LIB)
+        for name, res, args in SIGNATURES:
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+class SgwError(RuntimeError):
+    def __init__(self, status: int, where: str):
+        msg = lib().sgw_last_error().decode(errors="replace")
+        super().__init__(f"{where} failed with status {status}: {msg}")
+        self.status = status
+
+
+def check(status: int, where: str) -> int:
+    """Raise on API errors (negative status); return the reference ierr (>= 0)."""
+    if status < 0:
+        raise SgwError(status, where)
+    return status

@@ -1,0 +1,596 @@
+// C-ABI entry points of libsgw_gb300.so (declared in include/sgw_capi.h).
+#include <algorithm>
+#include <cmath>
+#include <map>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "host.cuh"
+#include "sgwsolver.cuh"
+
+namespace sgw {
+
+static thread_local std::string g_error;
+void set_error(const std::string& msg) { g_error = msg; }
+
+static sgw_status arg_error(const std::string& msg) {
+  set_error(msg);
+  return SGW_ERR_ARG;
+}
+
+// ---------------------------------------------------------------------------
+// FFT plans and twiddles
+// ---------------------------------------------------------------------------
+static bool make_plan(int n, FftPlan& p) {
+  if (n < 1 || n > kMaxFftLen) return false;
+  p.n = n;
+  p.nstage = 0;
+  p.rmin = 8;
+  int m = n;
+  for (int r : {8, 5, 4, 3, 2}) {
+    while (m % r == 0) {
+      if (p.nstage >= kMaxStages) return false;
+      p.radix[p.nstage++] = r;
+      p.rmin = std::min(p.rmin, r);
+      m /= r;
+    }
+  }
+  if (n == 1) {
+    p.radix[0] = 2;  // never used: a length-1 line is the identity
+    p.nstage = 0;
+    p.rmin = 1;
+  }
+  return m == 1;
+}
+
+template <typename T>
+static void twiddles(int n, std::vector<cplx<T>>& out) {
+  const long double pi = 3.14159265358979323846264338327950288L;
+  for (int e = 0; e < n; ++e) {
+    const long double ang = 2.0L * pi * (long double)e / (long double)n;
+    out.push_back(cplx<T>{(T)cosl(ang), (T)sinl(ang)});
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Launch-shape selection
+// ---------------------------------------------------------------------------
+template <typename T>
+static PwShape choose_shape(const PwView<T>& v, size_t smem_optin) {
+  const size_t static_bytes = sizeof(SeedShared) + 64;
+  const size_t budget = smem_optin > static_bytes ? smem_optin - static_bytes : 0;
+  PwShape s;
+  for (int ng : {4, 2, 1}) {
+    const size_t small = (size_t)pw_smem_small(v, ng) * sizeof(cplx<T>);
+    const size_t colb = (size_t)v.ncol * v.ldz * sizeof(cplx<T>);
+    if (small + colb <= budget) {
+      s.ng = ng;
+      s.col_in_smem = true;
+      s.smem = small + colb;
+      return s;
+    }
+  }
+  for (int ng : {4, 2, 1}) {
+    const size_t small = (size_t)pw_smem_small(v, ng) * sizeof(cplx<T>);
+    if (small <= budget) {
+      s.ng = ng;
+      s.col_in_smem = false;
+      s.smem = small;
+      return s;
+    }
+  }
+  s.ng = 0;
+  return s;
+}
+
+// ---------------------------------------------------------------------------
+// Operator construction
+// ---------------------------------------------------------------------------
+static sgw_status init_common(sgw_operator* op) {
+  SGW_CK(cudaGetDevice(&op->device));
+  cudaDeviceProp prop;
+  SGW_CK(cudaGetDeviceProperties(&prop, op->device));
+  op->num_sms = prop.multiProcessorCount;
+  op->smem_optin = prop.sharedMemPerBlockOptin;
+  SGW_CK(cudaStreamCreateWithFlags(&op->stream, cudaStreamNonBlocking));
+  SGW_CK(cudaEventCreate(&op->ev0));
+  SGW_CK(cudaEventCreate(&op->ev1));
+  return SGW_OK;
+}
+
+template <typename T>
+static sgw_status upload_pw(sgw_operator* op, const sgw_pw_operator_desc* d, const std::vector<int>& gcol_h,
+                            const std::vector<int>& gi3_h, const std::vector<int>& colpos_h,
+                            const std::vector<int>& i1_h, int ncol, int ldz, int pitch, const FftPlan& p1,
+                            const FftPlan& p2, const FftPlan& p3, DevBuf& g2k, DevBuf& vrs, DevBuf& vkb, DevBuf& dvan,
+                            DevBuf& evq, DevBuf& tw) {
+  const int npw = d->npw, npwx = op->npwx;
+  const size_t nnr = (size_t)d->nr1 * d->nr2 * d->nr3;
+  std::vector<T> g2(npw), vr(nnr), dv(std::max(d->nkb, 1));
+  for (int g = 0; g < npw; ++g) g2[g] = (T)d->g2kin[g];
+  for (size_t r = 0; r < nnr; ++r) vr[r] = (T)d->vrs[r];
+  for (int i = 0; i < d->nkb; ++i) dv[i] = (T)d->dvan[i];
+  std::vector<cplx<T>> kb((size_t)std::max(d->nkb, 1) * npwx, cplx<T>{0, 0});
+  for (int i = 0; i < d->nkb; ++i)
+    for (int g = 0; g < npw; ++g) {
+      const sgw_zcomplex z = d->vkb[(size_t)i * d->npwx + g];
+      kb[(size_t)i * npwx + g] = cplx<T>{(T)z.re, (T)z.im};
+    }
+  std::vector<cplx<T>> ev((size_t)std::max(d->nbnd_occ, 1) * npwx, cplx<T>{0, 0});
+  for (int v = 0; v < d->nbnd_occ; ++v)
+    for (int g = 0; g < npw; ++g) {
+      const sgw_zcomplex z = d->evq[(size_t)v * d->npwx + g];
+      ev[(size_t)v * npwx + g] = cplx<T>{(T)z.re, (T)z.im};
+    }
+  std::vector<cplx<T>> twv;
+  twiddles<T>(d->nr1, twv);
+  twiddles<T>(d->nr2, twv);
+  twiddles<T>(d->nr3, twv);
+  sgw_status s;
+  if ((s = g2k.upload(g2.data(), g2.size())) != SGW_OK) return s;
+  if ((s = vrs.upload(vr.data(), vr.size())) != SGW_OK) return s;
+  if ((s = vkb.upload(kb.data(), kb.size())) != SGW_OK) return s;
+  if ((s = dvan.upload(dv.data(), dv.size())) != SGW_OK) return s;
+  if ((s = evq.upload(ev.data(), ev.size())) != SGW_OK) return s;
+  if ((s = tw.upload(twv.data(), twv.size())) != SGW_OK) return s;
+  PwView<T>& v = pwview<T>(op);
+  v.npw = npw;
+  v.npwx = npwx;
+  v.nr1 = d->nr1;
+  v.nr2 = d->nr2;
+  v.nr3 = d->nr3;
+  v.nnr = (int)nnr;
+  v.ncol = ncol;
+  v.ni1 = (int)i1_h.size();
+  v.ldz = ldz;
+  v.pitch = pitch;
+  v.g_col = op->gcol.as<int>();
+  v.g_i3 = op->gi3.as<int>();
+  v.col_pos = op->colpos.as<int>();
+  v.i1_list = op->i1list.as<int>();
+  v.g2kin = g2k.as<T>();
+  v.vrs = vrs.as<T>();
+  v.nkb = d->nkb;
+  v.vkb = vkb.as<cplx<T>>();
+  v.dvan = dvan.as<T>();
+  v.nocc = d->nbnd_occ;
+  v.evq = evq.as<cplx<T>>();
+  v.alpha_pv = d->alpha_pv;
+  v.p1 = p1;
+  v.p2 = p2;
+  v.p3 = p3;
+  v.tw = tw.as<cplx<T>>();
+  pwshape<T>(op) = choose_shape(v, op->smem_optin);
+  return SGW_OK;
+}
+
+static sgw_status create_pw(const sgw_pw_operator_desc* d, sgw_operator** out) {
+  if (!d || !out) return arg_error("null argument");
+  if (d->npw < 1 || d->npwx < d->npw || d->nr1 < 1 || d->nr2 < 1 || d->nr3 < 1 || !d->nl || !d->g2kin || !d->vrs)
+    return arg_error("invalid plane-wave operator description");
+  if (d->nkb < 0 || (d->nkb > 0 && (!d->vkb || !d->dvan)) || d->nbnd_occ < 0 || (d->nbnd_occ > 0 && !d->evq))
+    return arg_error("invalid projector description");
+  FftPlan p1, p2, p3;
+  if (!make_plan(d->nr1, p1) || !make_plan(d->nr2, p2) || !make_plan(d->nr3, p3))
+    return arg_error("FFT dimensions must be 2,3,5-smooth and at most 64");
+  const long long nnr = (long long)d->nr1 * d->nr2 * d->nr3;
+  // sphere -> columns of the box
+  std::map<std::pair<int, int>, int> colmap;  // (i2, i1) -> column
+  std::vector<int> gcol(d->npw), gi3(d->npw);
+  std::vector<std::pair<int, int>> cols;
+  for (int g = 0; g < d->npw; ++g) {
+    const long long b = d->nl[g];
+    if (b < 0 || b >= nnr) return arg_error("nl index outside the FFT box");
+    const int i1 = (int)(b % d->nr1), i2 = (int)((b / d->nr1) % d->nr2), i3 = (int)(b / ((long long)d->nr1 * d->nr2));
+    auto key = std::make_pair(i2, i1);
+    auto it = colmap.find(key);
+    if (it == colmap.end()) it = colmap.emplace(key, 0).first;
+    gi3[g] = i3;
+    (void)it;
+  }
+  int c = 0;
+  for (auto& kv : colmap) {
+    kv.second = c++;
+    cols.push_back(kv.first);
+  }
+  for (int g = 0; g < d->npw; ++g) {
+    const long long b = d->nl[g];
+    const int i1 = (int)(b % d->nr1), i2 = (int)((b / d->nr1) % d->nr2);
+    gcol[g] = colmap[std::make_pair(i2, i1)];
+  }
+  // each box point may hold one sphere point only
+  {
+    std::vector<long long> seen(d->nl, d->nl + d->npw);
+    std::sort(seen.begin(), seen.end());
+    if (std::adjacent_find(seen.begin(), seen.end()) != seen.end()) return arg_error("duplicate nl index");
+  }
+  const int ncol = (int)cols.size();
+  const int ldz = d->nr3 | 1;
+  const int pitch = d->nr1 | 1;
+  std::vector<int> colpos(ncol);
+  std::vector<int> i1v;
+  for (int k = 0; k < ncol; ++k) {
+    colpos[k] = cols[k].second + pitch * cols[k].first;
+    i1v.push_back(cols[k].second);
+  }
+  std::sort(i1v.begin(), i1v.end());
+  i1v.erase(std::unique(i1v.begin(), i1v.end()), i1v.end());
+
+  sgw_operator* op = new sgw_operator();
+  op->kind = 1;
+  op->n = d->npw;
+  op->npwx = (d->npw + 31) / 32 * 32;
+  op->alpha_pv = d->alpha_pv;
+  sgw_status s = init_common(op);
+  if (s == SGW_OK) s = op->gcol.upload(gcol.data(), gcol.size());
+  if (s == SGW_OK) s = op->gi3.upload(gi3.data(), gi3.size());
+  if (s == SGW_OK) s = op->colpos.upload(colpos.data(), colpos.size());
+  if (s == SGW_OK) s = op->i1list.upload(i1v.data(), i1v.size());
+  if (s == SGW_OK)
+    s = upload_pw<double>(op, d, gcol, gi3, colpos, i1v, ncol, ldz, pitch, p1, p2, p3, op->g2k64, op->vrs64,
+                          op->vkb64, op->dvan64, op->evq64, op->tw64);
+  if (s == SGW_OK)
+    s = upload_pw<float>(op, d, gcol, gi3, colpos, i1v, ncol, ldz, pitch, p1, p2, p3, op->g2k32, op->vrs32,
+                         op->vkb32, op->dvan32, op->evq32, op->tw32);
+  if (s == SGW_OK && (op->shape64.ng == 0 || op->shape32.ng == 0)) {
+    set_error("FFT plane does not fit in shared memory");
+    s = SGW_ERR_UNSUPPORTED;
+  }
+  if (s != SGW_OK) {
+    sgw_operator_destroy(op);
+    return s;
+  }
+  *out = op;
+  return SGW_OK;
+}
+
+static sgw_status create_dense(int n, const sgw_zcomplex* a, long long lda, sgw_operator** out) {
+  if (!a || !out || n < 1 || lda < n) return arg_error("invalid dense operator");
+  sgw_operator* op = new sgw_operator();
+  op->kind = 0;
+  op->n = n;
+  op->npwx = (n + 31) / 32 * 32;
+  sgw_status s = init_common(op);
+  std::vector<zcd> h64((size_t)n * n);
+  std::vector<zcf> h32((size_t)n * n);
+  for (int j = 0; j < n; ++j)
+    for (int i = 0; i < n; ++i) {
+      const sgw_zcomplex z = a[(size_t)j * lda + i];
+      h64[(size_t)j * n + i] = zcd{z.re, z.im};
+      h32[(size_t)j * n + i] = zcf{(float)z.re, (float)z.im};
+    }
+  if (s == SGW_OK) s = op->a64.upload(h64.data(), h64.size());
+  if (s == SGW_OK) s = op->a32.upload(h32.data(), h32.size());
+  if (s != SGW_OK) {
+    sgw_operator_destroy(op);
+    return s;
+  }
+  op->dn64 = DenseView<double>{n, op->npwx, op->a64.as<zcd>()};
+  op->dn32 = DenseView<float>{n, op->npwx, op->a32.as<zcf>()};
+  *out = op;
+  return SGW_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Batched multishift BiCGStab(l) (device pointers)
+// ---------------------------------------------------------------------------
+static sgw_status check_batch(sgw_operator* op, const sgw_batch_desc* d) {
+  if (!op || !d) return arg_error("null argument");
+  if (d->nrhs < 0 || d->num_shift < 1 || d->lmax < 1 || d->lmax > kMaxL - 1 || d->max_iter < 1)
+    return arg_error("invalid batch sizes (num_shift >= 1, 1 <= lmax <= 15, max_iter >= 1)");
+  if (d->nrhs > 0 && (!d->bb || !d->sigma || !d->xx || !d->ierr)) return arg_error("null batch array");
+  if (d->ldb < op->n || d->lds < d->num_shift || d->ldx < op->n || d->ldr < d->ldx * (d->num_shift - 1) + op->n)
+    return arg_error("leading dimensions too small");
+  if (d->precision != 0 && d->precision != 1) return arg_error("precision must be 0 (FP64) or 1 (mixed)");
+  if (d->memory != 0 && d->memory != 1) return arg_error("memory must be 0 (host) or 1 (device)");
+  return SGW_OK;
+}
+
+sgw_status solve_mixed(sgw_operator* op, const BatchDev& b, int refine_max, double refine_thr);
+
+static sgw_status solve_batch_device(sgw_operator* op, const BatchDev& b, int precision, int refine_max,
+                                     double refine_thr) {
+  if (b.nrhs == 0) return SGW_OK;
+  if (precision == 0) return run_msbicg<double>(op, b);
+  return solve_mixed(op, b, refine_max, refine_thr);
+}
+
+static sgw_status solve_batch(sgw_operator* op, const sgw_batch_desc* d) {
+  sgw_status s = check_batch(op, d);
+  if (s != SGW_OK) return s;
+  op->last_launches = 0;
+  BatchDev b{d->nrhs, d->num_shift, d->lmax, d->max_iter, d->history_iters, d->threshold, nullptr, 0, nullptr, 0,
+             nullptr, 0, 0, nullptr, nullptr};
+  const int n = op->n, S = d->num_shift, R = d->nrhs;
+  std::vector<int> iters_h;
+  if (d->memory == 1) {
+    b.bb = d->bb;
+    b.ldb = d->ldb;
+    b.sigma = reinterpret_cast<const zcd*>(d->sigma);
+    b.lds = d->lds;
+    b.xx = d->xx;
+    b.ldx = d->ldx;
+    b.ldr = d->ldr;
+    b.ierr = d->ierr;
+    if ((s = op->st_iters.ensure(sizeof(int) * std::max(R, 1))) != SGW_OK) return s;
+    b.iters = d->iters ? d->iters : op->st_iters.as<int>();
+    SGW_CK(cudaEventRecord(op->ev0, op->stream));
+    s = solve_batch_device(op, b, d->precision, d->refine_max, d->refine_threshold);
+    if (s != SGW_OK) return s;
+    SGW_CK(cudaEventRecord(op->ev1, op->stream));
+    SGW_CK(cudaStreamSynchronize(op->stream));
+  } else {
+    // stage host arrays (packed) on the device, copies inside the timed call
+    if ((s = op->st_bb.ensure(sizeof(zcd) * (size_t)R * n)) != SGW_OK) return s;
+    if ((s = op->st_sigma.ensure(sizeof(zcd) * (size_t)R * S)) != SGW_OK) return s;
+    if ((s = op->st_xx.ensure(sizeof(zcd) * (size_t)R * S * n)) != SGW_OK) return s;
+    if ((s = op->st_ierr.ensure(sizeof(int) * R)) != SGW_OK) return s;
+    if ((s = op->st_iters.ensure(sizeof(int) * R)) != SGW_OK) return s;
+    SGW_CK(cudaEventRecord(op->ev0, op->stream));
+    SGW_CK(cudaMemcpy2DAsync(op->st_bb.p, sizeof(zcd) * n, d->bb, sizeof(zcd) * d->ldb, sizeof(zcd) * n, R,
+                             cudaMemcpyHostToDevice, op->stream));
+    SGW_CK(cudaMemcpy2DAsync(op->st_sigma.p, sizeof(zcd) * S, d->sigma, sizeof(zcd) * d->lds, sizeof(zcd) * S, R,
+                             cudaMemcpyHostToDevice, op->stream));
+    b.bb = op->st_bb.p;
+    b.ldb = n;
+    b.sigma = op->st_sigma.as<zcd>();
+    b.lds = S;
+    b.xx = op->st_xx.p;
+    b.ldx = n;
+    b.ldr = (long long)S * n;
+    b.ierr = op->st_ierr.as<int>();
+    b.iters = op->st_iters.as<int>();
+    s = solve_batch_device(op, b, d->precision, d->refine_max, d->refine_threshold);
+    if (s != SGW_OK) return s;
+    for (int r = 0; r < R; ++r)
+      SGW_CK(cudaMemcpy2DAsync(reinterpret_cast<zcd*>(d->xx) + (size_t)r * d->ldr, sizeof(zcd) * d->ldx,
+                               op->st_xx.as<zcd>() + (size_t)r * S * n, sizeof(zcd) * n, sizeof(zcd) * n, S,
+                               cudaMemcpyDeviceToHost, op->stream));
+    SGW_CK(cudaMemcpyAsync(d->ierr, op->st_ierr.p, sizeof(int) * R, cudaMemcpyDeviceToHost, op->stream));
+    if (d->iters) SGW_CK(cudaMemcpyAsync(d->iters, op->st_iters.p, sizeof(int) * R, cudaMemcpyDeviceToHost, op->stream));
+    SGW_CK(cudaEventRecord(op->ev1, op->stream));
+    SGW_CK(cudaStreamSynchronize(op->stream));
+  }
+  float ms = 0.f;
+  SGW_CK(cudaEventElapsedTime(&ms, op->ev0, op->ev1));
+  op->last_ms = ms;
+  return SGW_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Single right-hand side: bicgstab / linear_solver / select_solver
+// ---------------------------------------------------------------------------
+static sgw_status single_bicgstab(sgw_operator* op, int lmax, double thr, int max_iter, const sgw_zcomplex* bb, int n,
+                                  const sgw_zcomplex* sigma, int S, sgw_zcomplex* xx, long long ldx, int* ierr) {
+  if (!op || !bb || !sigma || !xx || !ierr) return arg_error("null argument");
+  if (n != op->n) return arg_error("right-hand side and operator sizes differ");
+  if (S < 1 || ldx < n) return arg_error("we need one solution vector per shift for the result");
+  sgw_batch_desc d{};
+  d.nrhs = 1;
+  d.num_shift = S;
+  d.lmax = lmax;
+  d.max_iter = max_iter;
+  d.threshold = thr;
+  d.precision = 0;
+  d.memory = 0;
+  d.bb = bb;
+  d.ldb = n;
+  d.sigma = sigma;
+  d.lds = S;
+  d.xx = xx;
+  d.ldx = ldx;
+  d.ldr = ldx * (S - 1) + n;
+  d.ierr = ierr;
+  d.iters = nullptr;
+  return solve_batch(op, &d);
+}
+
+static sgw_status single_sgw(sgw_operator* op, double thr, int max_iter, const sgw_zcomplex* bb, int n,
+                             const sgw_zcomplex* sigma, int S, sgw_zcomplex* xx, long long ldx, int* ierr) {
+  if (!op || !bb || !sigma || !xx || !ierr) return arg_error("null argument");
+  if (n != op->n) return arg_error("right-hand side and operator sizes differ");
+  if (S < 1 || ldx < n) return arg_error("invalid shifts or leading dimension");
+  op->last_launches = 0;
+  const int npwx = op->npwx;
+  const int kcap = std::min(std::min(max_iter, n), 4096) + 1;
+  sgw_status s;
+  DevBuf& w = op->ws64.vec;
+  if ((s = w.ensure(sizeof(zcd) * ((size_t)2 * kcap + 2) * npwx)) != SGW_OK) return s;
+  if ((s = op->st_bb.ensure(sizeof(zcd) * npwx)) != SGW_OK) return s;
+  if ((s = op->st_sigma.ensure(sizeof(zcd) * S)) != SGW_OK) return s;
+  if ((s = op->st_xx.ensure(sizeof(zcd) * (size_t)S * n)) != SGW_OK) return s;
+  if ((s = op->st_ierr.ensure(sizeof(int))) != SGW_OK) return s;
+  const long long colsz = col_elems<double>(op);
+  if (op->kind == 1 && !op->shape64.col_in_smem)
+    if ((s = op->ws64.col.ensure(sizeof(zcd) * colsz)) != SGW_OK) return s;
+  SGW_CK(cudaEventRecord(op->ev0, op->stream));
+  SGW_CK(cudaMemcpyAsync(op->st_bb.p, bb, sizeof(zcd) * n, cudaMemcpyHostToDevice, op->stream));
+  SGW_CK(cudaMemcpyAsync(op->st_sigma.p, sigma, sizeof(zcd) * S, cudaMemcpyHostToDevice, op->stream));
+  SgwArgs<double> a{};
+  a.threshold = thr;
+  a.max_iter = max_iter;
+  a.nshift = S;
+  a.npw = n;
+  a.npwx = npwx;
+  a.kcap = kcap;
+  a.bb = op->st_bb.as<zcd>();
+  a.sigma = op->st_sigma.as<zcd>();
+  a.xx = op->st_xx.as<zcd>();
+  a.ldx = n;
+  a.ierr = op->st_ierr.as<int>();
+  a.vv = w.as<zcd>();
+  a.ww = a.vv + (size_t)kcap * npwx;
+  a.res = a.ww + (size_t)kcap * npwx;
+  a.newv = a.res + npwx;
+  a.col_global = op->ws64.col.as<zcd>();
+  s = run_sgw<double>(op, a);
+  if (s != SGW_OK) return s;
+  SGW_CK(cudaMemcpy2DAsync(xx, sizeof(zcd) * ldx, op->st_xx.p, sizeof(zcd) * n, sizeof(zcd) * n, S,
+                           cudaMemcpyDeviceToHost, op->stream));
+  SGW_CK(cudaMemcpyAsync(ierr, op->st_ierr.p, sizeof(int), cudaMemcpyDeviceToHost, op->stream));
+  SGW_CK(cudaEventRecord(op->ev1, op->stream));
+  SGW_CK(cudaStreamSynchronize(op->stream));
+  float ms = 0.f;
+  SGW_CK(cudaEventElapsedTime(&ms, op->ev0, op->ev1));
+  op->last_ms = ms;
+  return SGW_OK;
+}
+
+static sgw_status apply_host(sgw_operator* op, sgw_zcomplex sigma, int m, const sgw_zcomplex* x, long long ldi,
+                             sgw_zcomplex* ax, long long ldo) {
+  if (!op || (m > 0 && (!x || !ax)) || m < 0 || ldi < op->n || ldo < op->n) return arg_error("invalid apply arguments");
+  if (m == 0) return SGW_OK;
+  const int n = op->n, npwx = op->npwx;
+  sgw_status s;
+  if ((s = op->st_misc.ensure(sizeof(zcd) * (size_t)m * npwx)) != SGW_OK) return s;
+  if ((s = op->st_misc2.ensure(sizeof(zcd) * (size_t)m * npwx)) != SGW_OK) return s;
+  SGW_CK(cudaMemsetAsync(op->st_misc.p, 0, sizeof(zcd) * (size_t)m * npwx, op->stream));
+  SGW_CK(cudaMemcpy2DAsync(op->st_misc.p, sizeof(zcd) * npwx, x, sizeof(zcd) * ldi, sizeof(zcd) * n, m,
+                           cudaMemcpyHostToDevice, op->stream));
+  s = run_apply<double>(op, m, op->st_misc.as<zcd>(), npwx, op->st_misc2.as<zcd>(), npwx, zcd{sigma.re, sigma.im});
+  if (s != SGW_OK) return s;
+  SGW_CK(cudaMemcpy2DAsync(ax, sizeof(zcd) * ldo, op->st_misc2.p, sizeof(zcd) * npwx, sizeof(zcd) * n, m,
+                           cudaMemcpyDeviceToHost, op->stream));
+  SGW_CK(cudaStreamSynchronize(op->stream));
+  return SGW_OK;
+}
+
+}  // namespace sgw
+
+// ---------------------------------------------------------------------------
+// extern "C"
+// ---------------------------------------------------------------------------
+using namespace sgw;
+
+extern "C" {
+
+sgw_status sgw_operator_create_pw(const sgw_pw_operator_desc* desc, sgw_operator** op) {
+  try {
+    return create_pw(desc, op);
+  } catch (...) {
+    set_error("host exception in sgw_operator_create_pw");
+    return SGW_ERR_NOMEM;
+  }
+}
+
+sgw_status sgw_operator_create_dense(int32_t n, const sgw_zcomplex* a, int64_t lda, sgw_operator** op) {
+  try {
+    return create_dense(n, a, lda, op);
+  } catch (...) {
+    set_error("host exception in sgw_operator_create_dense");
+    return SGW_ERR_NOMEM;
+  }
+}
+
+sgw_status sgw_operator_destroy(sgw_operator* op) {
+  if (!op) return SGW_OK;
+  if (op->stream) cudaStreamSynchronize(op->stream);
+  DevBuf* bufs[] = {&op->gcol, &op->gi3, &op->colpos, &op->i1list, &op->g2k64, &op->g2k32, &op->vrs64, &op->vrs32,
+                    &op->vkb64, &op->vkb32, &op->dvan64, &op->dvan32, &op->evq64, &op->evq32, &op->tw64, &op->tw32,
+                    &op->a64, &op->a32, &op->ws64.vec, &op->ws64.coef, &op->ws64.col, &op->ws64.counter,
+                    &op->ws32.vec, &op->ws32.coef, &op->ws32.col, &op->ws32.counter, &op->st_bb, &op->st_sigma,
+                    &op->st_xx, &op->st_ierr, &op->st_iters, &op->st_misc, &op->st_misc2, &op->st_misc3};
+  for (DevBuf* b : bufs) b->release();
+  if (op->ev0) cudaEventDestroy(op->ev0);
+  if (op->ev1) cudaEventDestroy(op->ev1);
+  if (op->stream) cudaStreamDestroy(op->stream);
+  delete op;
+  return SGW_OK;
+}
+
+sgw_status sgw_operator_set_alpha_pv(sgw_operator* op, double alpha_pv) {
+  if (!op) return arg_error("null operator");
+  op->alpha_pv = alpha_pv;
+  return SGW_OK;
+}
+
+sgw_status sgw_operator_apply(sgw_operator* op, sgw_zcomplex sigma, int32_t m, const sgw_zcomplex* x, int64_t ldx_in,
+                              sgw_zcomplex* ax, int64_t ldx_out) {
+  try {
+    return apply_host(op, sigma, m, x, ldx_in, ax, ldx_out);
+  } catch (...) {
+    set_error("host exception in sgw_operator_apply");
+    return SGW_ERR_NOMEM;
+  }
+}
+
+sgw_status sgw_bicgstab(sgw_operator* op, int32_t lmax, double threshold, int32_t max_iter, const sgw_zcomplex* bb,
+                        int32_t n, const sgw_zcomplex* sigma, int32_t num_shift, sgw_zcomplex* xx, int64_t ldx,
+                        int32_t* ierr) {
+  try {
+    sgw_status s = single_bicgstab(op, lmax, threshold, max_iter, bb, n, sigma, num_shift, xx, ldx, ierr);
+    return s == SGW_OK ? (sgw_status)*ierr : s;
+  } catch (...) {
+    set_error("host exception in sgw_bicgstab");
+    return SGW_ERR_NOMEM;
+  }
+}
+
+sgw_status sgw_linear_solver(sgw_operator* op, double threshold, int32_t max_iter, const sgw_zcomplex* bb, int32_t n,
+                             const sgw_zcomplex* sigma, int32_t num_shift, sgw_zcomplex* xx, int64_t ldx,
+                             int32_t* ierr) {
+  try {
+    sgw_status s = single_sgw(op, threshold, max_iter, bb, n, sigma, num_shift, xx, ldx, ierr);
+    return s == SGW_OK ? (sgw_status)*ierr : s;
+  } catch (...) {
+    set_error("host exception in sgw_linear_solver");
+    return SGW_ERR_NOMEM;
+  }
+}
+
+// select_solver.f90:67-161: try the solvers in priority order until ierr == 0.
+sgw_status sgw_select_solver(sgw_operator* op, const sgw_solver_config* cfg, const sgw_zcomplex* bb, int32_t n,
+                             const sgw_zcomplex* sigma, int32_t num_shift, sgw_zcomplex* xx, int64_t ldx,
+                             int32_t* ierr) {
+  if (!cfg || !ierr) return arg_error("null argument");
+  if (cfg->num_priority < 1 || cfg->num_priority > 8)
+    return arg_error("priority of the solvers not specified");  // select_solver.f90:116-118
+  *ierr = 1;
+  for (int k = 0; k < cfg->num_priority; ++k) {
+    sgw_status s = SGW_OK;
+    switch (cfg->priority[k]) {
+      case SGW_BICGSTAB_MULTI:
+        s = sgw_bicgstab(op, cfg->bicg_lmax, cfg->threshold, cfg->max_iter, bb, n, sigma, num_shift, xx, ldx, ierr);
+        break;
+      case SGW_BICGSTAB_NO_MULTI:
+        // the reference solves the full shift list once per shift (select_solver.f90:144-146)
+        for (int r = 0; r < num_shift; ++r) {
+          s = sgw_bicgstab(op, cfg->bicg_lmax, cfg->threshold, cfg->max_iter, bb, n, sigma, num_shift, xx, ldx, ierr);
+          if (s < 0) break;
+        }
+        break;
+      case SGW_SGW_LINEAR_SOLVER:
+        s = sgw_linear_solver(op, cfg->threshold, cfg->max_iter, bb, n, sigma, num_shift, xx, ldx, ierr);
+        break;
+      default:
+        break;
+    }
+    if (s < 0) return s;
+    if (*ierr == 0) break;
+  }
+  return (sgw_status)*ierr;
+}
+
+sgw_status sgw_solve_batch(sgw_operator* op, const sgw_batch_desc* desc) {
+  try {
+    return solve_batch(op, desc);
+  } catch (...) {
+    set_error("host exception in sgw_solve_batch");
+    return SGW_ERR_NOMEM;
+  }
+}
+
+sgw_status sgw_last_timing(sgw_operator* op, double* ms, int64_t* launches) {
+  if (!op) return arg_error("null operator");
+  if (ms) *ms = op->last_ms;
+  if (launches) *launches = op->last_launches;
+  return SGW_OK;
+}
+
+const char* sgw_last_error(void) { return g_error.c_str(); }
+
+const char* sgw_version(void) { return "sgw_gb300 0.1 (sm_103a)"; }
+
+}  // extern "C"
+

@@ -1,0 +1,138 @@
+// Host-side state of an operator handle and its workspaces.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/sgw_capi.h"
+#include "msbicg.cuh"
+#include "sgwsolver.cuh"
+
+namespace sgw {
+
+void set_error(const std::string& msg);
+
+#define SGW_CK(call)                                                                        \
+  do {                                                                                      \
+    cudaError_t e_ = (call);                                                                \
+    if (e_ != cudaSuccess) {                                                                \
+      ::sgw::set_error(std::string(#call) + " failed: " + cudaGetErrorString(e_));          \
+      return SGW_ERR_CUDA;                                                                  \
+    }                                                                                       \
+  } while (0)
+
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  sgw_status ensure(size_t want) {
+    if (want <= bytes && p) return SGW_OK;
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+    if (want == 0) want = 16;
+    cudaError_t e = cudaMalloc(&p, want);
+    if (e != cudaSuccess) {
+      p = nullptr;
+      set_error(std::string("cudaMalloc(") + std::to_string(want) + ") failed: " + cudaGetErrorString(e));
+      return e == cudaErrorMemoryAllocation ? SGW_ERR_NOMEM : SGW_ERR_CUDA;
+    }
+    bytes = want;
+    return SGW_OK;
+  }
+  template <typename T> sgw_status upload(const T* host, size_t count) {
+    sgw_status s = ensure(count * sizeof(T));
+    if (s != SGW_OK) return s;
+    if (count) SGW_CK(cudaMemcpy(p, host, count * sizeof(T), cudaMemcpyHostToDevice));
+    return SGW_OK;
+  }
+  template <typename T> T* as() const { return reinterpret_cast<T*>(p); }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+  }
+};
+
+// Pruned-FFT launch shape of a plane-wave operator in one precision.
+struct PwShape {
+  int ng = 1;            // plane groups
+  bool col_in_smem = true;
+  size_t smem = 0;       // dynamic shared memory bytes
+};
+
+// A batch with every array already in device memory.
+struct BatchDev {
+  int nrhs, nshift, lmax, max_iter, history_iters;
+  double threshold;
+  const void* bb;
+  long long ldb;
+  const zcd* sigma;
+  long long lds;
+  void* xx;
+  long long ldx, ldr;
+  int* ierr;
+  int* iters;
+};
+
+struct Workspace {
+  DevBuf vec, coef, col, counter;
+};
+
+}  // namespace sgw
+
+struct sgw_operator {
+  int kind = 0;  // 0 dense, 1 plane-wave
+  int n = 0, npwx = 0;
+  int device = 0, num_sms = 0;
+  size_t smem_optin = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  double last_ms = 0.0;
+  long long last_launches = 0;
+  double alpha_pv = 0.0;
+  // tables
+  sgw::DevBuf gcol, gi3, colpos, i1list, g2k64, g2k32, vrs64, vrs32, vkb64, vkb32, dvan64, dvan32, evq64, evq32,
+      tw64, tw32, a64, a32;
+  sgw::PwView<double> pw64{};
+  sgw::PwView<float> pw32{};
+  sgw::DenseView<double> dn64{};
+  sgw::DenseView<float> dn32{};
+  sgw::PwShape shape64, shape32;
+  // workspaces and staging
+  sgw::Workspace ws64, ws32;
+  sgw::DevBuf st_bb, st_sigma, st_xx, st_ierr, st_iters, st_misc, st_misc2, st_misc3;
+};
+
+namespace sgw {
+template <typename T> struct Ipt;
+template <> struct Ipt<double> { static constexpr int v = 2; };
+template <> struct Ipt<float> { static constexpr int v = 4; };
+
+template <typename T> PwView<T>& pwview(sgw_operator* op);
+template <> inline PwView<double>& pwview<double>(sgw_operator* op) { return op->pw64; }
+template <> inline PwView<float>& pwview<float>(sgw_operator* op) { return op->pw32; }
+template <typename T> DenseView<T>& dnview(sgw_operator* op);
+template <> inline DenseView<double>& dnview<double>(sgw_operator* op) { return op->dn64; }
+template <> inline DenseView<float>& dnview<float>(sgw_operator* op) { return op->dn32; }
+template <typename T> PwShape& pwshape(sgw_operator* op);
+template <> inline PwShape& pwshape<double>(sgw_operator* op) { return op->shape64; }
+template <> inline PwShape& pwshape<float>(sgw_operator* op) { return op->shape32; }
+template <typename T> Workspace& wsp(sgw_operator* op);
+template <> inline Workspace& wsp<double>(sgw_operator* op) { return op->ws64; }
+template <> inline Workspace& wsp<float>(sgw_operator* op) { return op->ws32; }
+
+template <typename T>
+inline long long col_elems(sgw_operator* op) {
+  return op->kind == 1 ? (long long)pwview<T>(op).ncol * pwview<T>(op).ldz : 0;
+}
+
+
+template <typename T> sgw_status run_msbicg(sgw_operator* op, const BatchDev& b);
+template <typename T> sgw_status run_sgw(sgw_operator* op, const SgwArgs<T>& a);
+template <typename T>
+sgw_status run_apply(sgw_operator* op, int m, const cplx<T>* x, long long ldi, cplx<T>* ax, long long ldo, zcd sigma);
+sgw_status solve_mixed(sgw_operator* op, const BatchDev& b, int refine_max, double refine_thr);
+}  // namespace sgw

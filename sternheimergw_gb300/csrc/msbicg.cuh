@@ -1,0 +1,639 @@
+// Persistent multishift BiCGStab(l) (bicgstab.f90:154-999, Frommer's shifted
+// BiCGStab(l)) for a batch of right-hand sides.
+//
+// Work split: one CTA owns one right-hand side at a time and takes the next
+// from an atomic work queue when it is done, so converged systems leave the
+// machine in place and uneven systems balance themselves.  A CTA's working set
+// (the seed vectors u_0..u_l, r_0..r_l, x, r~0) lives in a per-CTA slot of
+// global memory that stays in L2 while the CTA works on it.
+//
+// The seed system runs exactly as in the reference with explicit vectors: the
+// unconjugated dots, the delayed alpha_old and r_0 updates, and the seed-only
+// absolute convergence test (bicgstab.f90:237,245,278-301).
+//
+// The shifted systems never touch a vector during the iteration.  In the
+// reference every shifted vector (u_i^sigma, x^sigma) is a linear
+// combination of seed vectors and of the shift's own u_0^sigma from the start
+// of the outer iteration, with coefficients that depend on seed scalars only
+// (bicgstab.f90:621-664, :688-698, :850-913).  So each outer iteration stores
+// a basis of 2l+2 seed vectors (r_0 and u_0 at its start, and the 2l operator
+// outputs u_{j+1} = A u_j, r_{j+1} = A r_j), and every shift replays the
+// reference's updates on coefficient vectors over that basis plus one carry
+// coordinate for u_0^sigma (FP64, one thread per shift).  x^sigma is formed
+// once at the end as  X = W F  (basis x coefficients).  When the history slot
+// fills up, x^sigma and u_0^sigma are materialised and a new window begins.
+// This turns the reference's O(l^2 S n) vector traffic per iteration into
+// O(l^2 S) scalar work plus one (n x K) (K x S) product per system.
+#pragma once
+#include "cplx.cuh"
+#include "pwop.cuh"
+
+namespace sgw {
+
+constexpr int kMaxL = 16;
+constexpr int kThreads = 512;
+
+template <typename T>
+struct SolverArgs {
+  int lmax, max_iter;
+  double threshold;
+  int nshift, nrhs, npw, npwx;
+  const cplx<T>* bb;   // [rhs] stride ldb
+  long long ldb;
+  const zcd* sigma;    // [rhs] stride lds, nshift values
+  long long lds;
+  cplx<T>* xx;         // x[rhs * ldr + shift * ldx + g]
+  long long ldx, ldr;
+  int* ierr;           // [rhs]
+  int* iters;          // [rhs]
+  int* counter;        // work queue head
+  // per-CTA slot workspace
+  cplx<T>* ws_vec;     // [slot][nvec_slot][npwx]
+  long long nvec_slot;
+  zcd* ws_coef;        // [slot][ncoef_slot]
+  long long ncoef_slot;
+  int Kcap;            // history vectors per window
+  int P;               // padded shift count (multiple of 32)
+  cplx<T>* col_global; // [slot][ncol*ldz] when the column store does not fit in shared memory
+  long long col_slot;
+  int mode;            // 0 coefficient-space shifts, 1 explicit shift vectors
+};
+
+// Shared seed scalars of the MR part (tau, nu, gammas), 1-based like the reference.
+struct SeedShared {
+  zcd tau[(kMaxL + 1) * (kMaxL + 2) / 2];
+  zcd nu[kMaxL + 1];
+  zcd gamma[kMaxL + 1];
+  zcd gamma_p[kMaxL + 1];
+  zcd gamma_pp[kMaxL + 1];
+  zcd red[32];
+  int flag;
+};
+
+#define SGW_MUIDX(j, i) ((j) * ((j) + 1) / 2 + (i))
+#define SGW_TAUIDX(j, i) ((j) * ((j) + 1) / 2 + (i))
+
+// Layout of the FP64 coefficient slot (all per-shift arrays are [field][P]).
+struct CoefLayout {
+  int l, D, Db, P, Kcap;
+  long long o_scal, o_mu, o_us, o_xinc, o_xa, o_ub, o_gs, o_gp, o_gpp, o_cr, o_cu, total;
+  __host__ __device__ CoefLayout(int l_, int P_, int Kcap_) : l(l_), P(P_), Kcap(Kcap_) {
+    D = 2 * l + 3;
+    Db = 2 * l + 2;
+    long long o = 0;
+    o_scal = o; o += 10LL * P;                      // the SC_* scalars
+    o_mu = o; o += (long long)(l * (l + 1) / 2) * P;
+    o_us = o; o += (long long)(l + 1) * D * P;
+    o_xinc = o; o += (long long)D * P;
+    o_xa = o; o += (long long)Kcap * P;
+    o_ub = o; o += (long long)Kcap * P;
+    o_gs = o; o += (long long)(l + 1) * P;
+    o_gp = o; o += (long long)(l + 1) * P;
+    o_gpp = o; o += (long long)(l + 1) * P;
+    o_cr = o; o += (long long)(l + 1) * Db;          // seed coefficient vectors (shared by the CTA)
+    o_cu = o; o += (long long)(l + 1) * Db;
+    total = o;
+  }
+};
+
+enum { SC_PHIOLD = 0, SC_PHI, SC_THETA, SC_SIG, SC_ALPHA, SC_UC, SC_XD, SC_BETA, SC_F1, SC_F2 };
+
+// --- operator adaptors -------------------------------------------------------
+
+template <typename T, int IPT>
+struct PwApply {
+  PwView<T> op;
+  bool col_in_smem;
+  int ng;  // plane groups
+  __device__ int smem_small() const { return pw_smem_small(op, ng); }
+  __device__ void setup(cplx<T>* sm) const {
+    for (int e = threadIdx.x; e < op.nr1 + op.nr2 + op.nr3; e += blockDim.x) sm[e] = op.tw[e];
+    __syncthreads();
+  }
+  __device__ void apply(const cplx<T>* in, cplx<T>* out, cplx<T>* out2, zcd sigma, cplx<T>* sm, cplx<T>* col) const {
+    pw_apply_cta<T, IPT>(op, ng, in, out, out2, sigma, sm, col);
+  }
+};
+
+template <typename T>
+struct DenseApply {
+  DenseView<T> op;
+  bool col_in_smem;
+  __device__ int smem_small() const { return op.n; }
+  __device__ void setup(cplx<T>*) const {}
+  __device__ void apply(const cplx<T>* in, cplx<T>* out, cplx<T>* out2, zcd sigma, cplx<T>* sm, cplx<T>*) const {
+    dense_apply_cta<T>(op, in, out, out2, sigma, sm);
+  }
+};
+
+// --- small CTA-wide vector helpers ------------------------------------------
+
+template <typename T>
+__device__ __forceinline__ void v_copy(cplx<T>* y, const cplx<T>* x, int n) {
+  for (int g = threadIdx.x; g < n; g += blockDim.x) y[g] = x[g];
+}
+template <typename T>
+__device__ __forceinline__ void v_axpy(cplx<T>* y, zcd a, const cplx<T>* x, int n) {
+  const cplx<T> aa = ccast<T>(a);
+  for (int g = threadIdx.x; g < n; g += blockDim.x) y[g] += aa * x[g];
+}
+
+// --- the coefficient-space replay of one shifted system ---------------------
+// Per-shift arrays are strided by P (thread s touches column s).
+
+struct ShiftRef {
+  zcd* base;
+  int s, P;
+  __device__ zcd& at(long long off, int idx) const { return base[off + (long long)idx * P + s]; }
+};
+
+// Scalar recurrences of one shifted system (FP64, one thread per shift).  The
+// vector updates that use them run either on coefficient vectors (mode 0) or
+// on explicit shift vectors (mode 1).
+
+// bicgstab.f90:625-638 and :655-657 at BiCG step j.
+__device__ inline void shift_bicg_scalars(const ShiftRef& sh, const CoefLayout& L, zcd alpha, zcd beta, zcd alpha_old) {
+  const zcd one = {1.0, 0.0};
+  zcd& inv_phi_old = sh.at(L.o_scal, SC_PHIOLD);
+  zcd& inv_phi = sh.at(L.o_scal, SC_PHI);
+  const zcd sig = sh.at(L.o_scal, SC_SIG);
+  const zcd inv_phi_new = inv_phi / (one + alpha * sig + alpha * beta / alpha_old * (inv_phi / inv_phi_old - one));
+  const zcd ratio = inv_phi / inv_phi_old;
+  sh.at(L.o_scal, SC_BETA) = ratio * ratio * beta;
+  sh.at(L.o_scal, SC_ALPHA) = (inv_phi_new / inv_phi) * alpha;
+  sh.at(L.o_scal, SC_F1) = sh.at(L.o_scal, SC_THETA) * inv_phi;  // 1/(theta phi) of L15/L19
+  inv_phi_old = inv_phi;
+  inv_phi = inv_phi_new;
+  sh.at(L.o_scal, SC_F2) = -sh.at(L.o_scal, SC_THETA) * inv_phi;  // L26 factor (updated phi)
+}
+
+// Horner's scheme (bicgstab.f90:941-999), gs 1-based.
+__device__ inline void replay_horner(const ShiftRef& sh, const CoefLayout& L, const zcd* gamma, zcd sigma, zcd& psi) {
+  const int l = L.l;
+  sh.at(L.o_gs, l) = -gamma[l];
+  for (int jj = l - 1; jj >= 1; --jj) sh.at(L.o_gs, jj) = -sigma * sh.at(L.o_gs, jj + 1) - gamma[jj];
+  psi = -sigma * sh.at(L.o_gs, 1) + zcd{1.0, 0.0};
+  for (int ii = 1; ii <= l - 1; ++ii)
+    for (int jj = l - 1; jj >= ii; --jj) sh.at(L.o_gs, jj) = -sigma * sh.at(L.o_gs, jj + 1) + sh.at(L.o_gs, jj);
+  for (int jj = 1; jj <= l; ++jj) sh.at(L.o_gs, jj) = -sh.at(L.o_gs, jj) / psi;
+}
+
+// bicgstab.f90:854-884: MR scalars of one shift.  Leaves the x-update factors
+// gamma_1'^/xi and gamma_j''^/xi in o_gpp[0..l-1] and 1/psi in SC_F1.
+__device__ inline void shift_mr_scalars(const ShiftRef& sh, const CoefLayout& L, const SeedShared& ss) {
+  const int l = L.l;
+  zcd psi;
+  replay_horner(sh, L, ss.gamma, sh.at(L.o_scal, SC_SIG), psi);
+  zcd& inv_theta = sh.at(L.o_scal, SC_THETA);
+  const zcd inv_xi = inv_theta * sh.at(L.o_scal, SC_PHI);
+  inv_theta = inv_theta / psi;
+  for (int jj = 1; jj <= l; ++jj) {
+    zcd acc = {0.0, 0.0};
+    for (int ii = jj; ii <= l; ++ii) acc += sh.at(L.o_mu, SGW_MUIDX(ii - 1, jj - 1)) * sh.at(L.o_gs, ii);
+    sh.at(L.o_gp, jj) = acc;
+  }
+  for (int jj = 1; jj <= l - 1; ++jj) {
+    zcd acc = sh.at(L.o_gp, jj + 1);
+    for (int ii = jj + 1; ii <= l - 1; ++ii) acc += ss.tau[SGW_TAUIDX(ii, jj)] * sh.at(L.o_gp, ii + 1);
+    sh.at(L.o_gpp, jj) = acc * inv_xi;
+  }
+  sh.at(L.o_gpp, 0) = sh.at(L.o_gp, 1) * inv_xi;
+  sh.at(L.o_scal, SC_F1) = zcd{1.0, 0.0} / psi;
+}
+
+// Mode 0: the shift's vector updates on coefficient vectors (cr = seed r_i).
+// bicgstab.f90:641-662 at step j, before the seed's r update.
+__device__ inline void replay_bicg1(const ShiftRef& sh, const CoefLayout& L, const zcd* cr, int j) {
+  const zcd beta_s = sh.at(L.o_scal, SC_BETA), alpha_s = sh.at(L.o_scal, SC_ALPHA), factor = sh.at(L.o_scal, SC_F1);
+  const int D = L.D, Db = L.Db;
+  for (int i = 0; i <= j; ++i) {  // L15: u_i = -beta u_i + factor r_i
+    for (int q = 0; q < Db; ++q) {
+      zcd& u = sh.at(L.o_us, i * D + q);
+      u = -beta_s * u;
+      u += factor * cr[i * Db + q];
+    }
+    zcd& uc = sh.at(L.o_us, i * D + Db);
+    uc = -beta_s * uc;
+  }
+  for (int q = 0; q < D; ++q) sh.at(L.o_xinc, q) += alpha_s * sh.at(L.o_us, q);  // L17
+  for (int q = 0; q < Db; ++q) sh.at(L.o_us, (j + 1) * D + q) = factor * cr[j * Db + q];  // L19
+  sh.at(L.o_us, (j + 1) * D + Db) = zcd{0.0, 0.0};
+}
+
+// bicgstab.f90:692-696 after the seed's r update of step j.
+__device__ inline void replay_bicg2(const ShiftRef& sh, const CoefLayout& L, const zcd* cr, int j) {
+  const zcd factor = sh.at(L.o_scal, SC_F2);
+  const zcd inv_alpha = zcd{1.0, 0.0} / sh.at(L.o_scal, SC_ALPHA);
+  const zcd msig = -sh.at(L.o_scal, SC_SIG);
+  const int D = L.D, Db = L.Db;
+  for (int q = 0; q < D; ++q) {
+    zcd u = sh.at(L.o_us, (j + 1) * D + q);
+    if (q < Db) u += factor * cr[j * Db + q];
+    u = inv_alpha * u;
+    u += msig * sh.at(L.o_us, j * D + q);
+    sh.at(L.o_us, (j + 1) * D + q) = u;
+  }
+}
+
+// bicgstab.f90:886-911 on coefficient vectors; cr holds the seed r_j after Gram-Schmidt.
+__device__ inline void replay_mr(const ShiftRef& sh, const CoefLayout& L, const zcd* cr, const SeedShared& ss) {
+  const int l = L.l, D = L.D, Db = L.Db;
+  const zcd f0 = sh.at(L.o_gpp, 0);
+  for (int q = 0; q < Db; ++q) sh.at(L.o_xinc, q) += f0 * cr[q];
+  for (int q = 0; q < D; ++q) sh.at(L.o_us, q) += (-ss.gamma[l]) * sh.at(L.o_us, l * D + q);
+  for (int jj = 1; jj <= l - 1; ++jj) {
+    for (int q = 0; q < D; ++q) sh.at(L.o_us, q) += (-ss.gamma[jj]) * sh.at(L.o_us, jj * D + q);
+    const zcd f = sh.at(L.o_gpp, jj);
+    for (int q = 0; q < Db; ++q) sh.at(L.o_xinc, q) += f * cr[jj * Db + q];
+  }
+  const zcd ipsi = sh.at(L.o_scal, SC_F1);  // L34
+  for (int q = 0; q < D; ++q) sh.at(L.o_us, q) = ipsi * sh.at(L.o_us, q);
+}
+
+// Fold the finished outer iteration (basis block at kw) into the window
+// accumulators: x_inc over the window (XA, Xd) and u_0^sigma (UB, Uc).
+__device__ inline void replay_window(const ShiftRef& sh, const CoefLayout& L, int kw) {
+  const int D = L.D, Db = L.Db;
+  const zcd d = sh.at(L.o_xinc, Db);
+  const zcd c = sh.at(L.o_us, Db);
+  zcd& Uc = sh.at(L.o_scal, SC_UC);
+  zcd& Xd = sh.at(L.o_scal, SC_XD);
+  for (int k = 0; k < kw; ++k) {
+    zcd& ub = sh.at(L.o_ub, k);
+    sh.at(L.o_xa, k) += d * ub;
+    ub = c * ub;
+  }
+  Xd += d * Uc;
+  Uc = c * Uc;
+  for (int q = 0; q < Db; ++q) {
+    sh.at(L.o_xa, kw + q) = sh.at(L.o_xinc, q);
+    sh.at(L.o_ub, kw + q) = sh.at(L.o_us, q);
+  }
+  (void)D;
+}
+
+// y[s][g] (+)= sum_k W[k][g] C[k][s] + carry[s] * Z[s][g], for all shifts s < ns.
+// W: [K][npwx]; C: FP64 [k*P + s]; Z: [s][npwx] (may be null).
+template <typename T>
+__device__ void cta_basis_gemm(cplx<T>* y, long long ldy, bool accumulate, const cplx<T>* W, int K, const zcd* C,
+                               int P, const zcd* carry, const cplx<T>* Z, int ns, int n, int npwx) {
+  constexpr int GL = 128;               // rows per tile
+  constexpr int QMAX = 16;              // shifts per thread per pass
+  const int sgrp = blockDim.x / GL;     // shift groups
+  const int gl = threadIdx.x % GL, sg = threadIdx.x / GL;
+  for (int s0 = 0; s0 < ns; s0 += sgrp * QMAX) {
+    for (int g0 = 0; g0 < n; g0 += GL) {
+      const int g = g0 + gl;
+      cplx<T> acc[QMAX];
+#pragma unroll
+      for (int q = 0; q < QMAX; ++q) acc[q] = cplx<T>{0, 0};
+      if (g < n) {
+        for (int k = 0; k < K; ++k) {
+          const cplx<T> w = W[(size_t)k * npwx + g];
+          const zcd* ck = C + (size_t)k * P;
+#pragma unroll
+          for (int q = 0; q < QMAX; ++q) {
+            const int s = s0 + sg + q * sgrp;
+            if (s < ns) acc[q] += w * ccast<T>(ck[s]);
+          }
+        }
+#pragma unroll
+        for (int q = 0; q < QMAX; ++q) {
+          const int s = s0 + sg + q * sgrp;
+          if (s < ns) {
+            cplx<T> v = acc[q];
+            if (Z) v += ccast<T>(carry[s]) * Z[(size_t)s * npwx + g];
+            cplx<T>* dst = y + (size_t)s * ldy + g;
+            *dst = accumulate ? *dst + v : v;
+          }
+        }
+      }
+    }
+  }
+}
+
+// --- the solve of one right-hand side -------------------------------------
+// mode 0: shifted systems in coefficient space over the history basis.
+// mode 1: shifted systems as explicit vectors (the reference's own recurrence,
+//         used for long MR cycles where the coefficient form loses accuracy).
+
+template <typename T, class ApplyT>
+__device__ void solve_one(const SolverArgs<T>& a, const ApplyT& A, int rhs, int slot, cplx<T>* sm, cplx<T>* col,
+                          SeedShared& ss) {
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const int n = a.npw, npwx = a.npwx, l = a.lmax, S = a.nshift, Sm1 = S - 1;
+  const CoefLayout L(l, a.P, a.Kcap);
+  const int Db = L.Db;
+  const bool explicit_mode = a.mode == 1;
+  const bool track = Sm1 > 0 && !explicit_mode;
+
+  cplx<T>* V = a.ws_vec + (size_t)slot * a.nvec_slot * npwx;
+  cplx<T>* U = V;
+  cplx<T>* R = V + (size_t)(l + 1) * npwx;
+  cplx<T>* X = V + (size_t)(2 * l + 2) * npwx;
+  cplx<T>* TR0 = X + npwx;
+  cplx<T>* W = TR0 + npwx;                      // mode 0: history basis (Kcap vectors)
+  cplx<T>* U0S = W + (size_t)a.Kcap * npwx;     // mode 0: u_0^sigma carry after a flush
+  cplx<T>* US = TR0 + npwx;                     // mode 1: u_i^sigma [s][i][npwx]
+  cplx<T>* XS = US + (size_t)Sm1 * (l + 1) * npwx;  // mode 1: x^sigma [s][npwx]
+  zcd* C = a.ws_coef + (size_t)slot * a.ncoef_slot;
+  zcd* cr = C + L.o_cr;
+  zcd* cu = C + L.o_cu;
+#define UV(i) (U + (size_t)(i) * npwx)
+#define RV(i) (R + (size_t)(i) * npwx)
+#define USV(s, i) (US + ((size_t)(s) * (l + 1) + (i)) * npwx)
+#define XSV(s) (XS + (size_t)(s) * npwx)
+#define SCAL(s, f) C[L.o_scal + (long long)(f) * L.P + (s)]
+
+  const cplx<T>* bb = a.bb + (size_t)rhs * a.ldb;
+  const zcd* sigma = a.sigma + (size_t)rhs * a.lds;
+  cplx<T>* xout = a.xx + (size_t)rhs * a.ldr;
+  const zcd sigma_seed = sigma[0];
+
+  // init_seed (bicgstab.f90:304-350)
+  for (int g = tid; g < npwx; g += nt) {
+    const cplx<T> b = g < n ? bb[g] : cplx<T>{0, 0};
+    RV(0)[g] = b;
+    TR0[g] = b;
+    UV(0)[g] = cplx<T>{0, 0};
+    X[g] = cplx<T>{0, 0};
+  }
+  if (explicit_mode)
+    for (long long e = tid; e < (long long)Sm1 * npwx; e += nt) {
+      const int s = (int)(e / npwx), g = (int)(e - (long long)s * npwx);
+      USV(s, 0)[g] = cplx<T>{0, 0};
+      XSV(s)[g] = cplx<T>{0, 0};
+    }
+  zcd rho_old = {1.0, 0.0}, alpha_old = {1.0, 0.0}, alpha = {0.0, 0.0}, omega = {1.0, 0.0}, beta = {0.0, 0.0};
+  // init_shift (bicgstab.f90:370-490), one thread per shift
+  for (int s = tid; s < Sm1; s += nt) {
+    const ShiftRef sh{C, s, L.P};
+    sh.at(L.o_scal, SC_PHIOLD) = zcd{1.0, 0.0};
+    sh.at(L.o_scal, SC_PHI) = zcd{1.0, 0.0};
+    sh.at(L.o_scal, SC_THETA) = zcd{1.0, 0.0};
+    const zcd sg = sigma[s + 1] - sigma_seed;
+    sh.at(L.o_scal, SC_SIG) = sg;
+    sh.at(L.o_scal, SC_UC) = zcd{1.0, 0.0};
+    sh.at(L.o_scal, SC_XD) = zcd{0.0, 0.0};
+    // mu_ij = C(j, i) sigma^(j-i); binomials by the recurrence of :423-431
+    for (int jj = 0; jj < l; ++jj) {
+      double binom = 1.0;
+      for (int ii = 0; ii <= jj; ++ii) {
+        if (ii > 0) binom = (binom * (jj - ii + 1)) / ii;
+        zcd p = {1.0, 0.0};
+        for (int e = 0; e < jj - ii; ++e) p = sg * p;
+        sh.at(L.o_mu, SGW_MUIDX(jj, ii)) = binom * p;
+      }
+    }
+    for (int k = 0; k < a.Kcap; ++k) {
+      sh.at(L.o_xa, k) = zcd{0.0, 0.0};
+      sh.at(L.o_ub, k) = zcd{0.0, 0.0};
+    }
+  }
+  __syncthreads();
+
+  int kw = 0;
+  bool flushed = false;
+  bool conv = false;
+  int iter;
+  for (iter = 1; iter <= a.max_iter; ++iter) {
+    if (track && kw + Db > a.Kcap) {
+      // materialise x^sigma and u_0^sigma, start a new window
+      cta_basis_gemm<T>(xout + a.ldx, a.ldx, flushed, W, kw, C + L.o_xa, L.P, C + L.o_scal + SC_XD * L.P,
+                        flushed ? U0S : nullptr, Sm1, n, npwx);
+      cta_basis_gemm<T>(U0S, npwx, false, W, kw, C + L.o_ub, L.P, C + L.o_scal + SC_UC * L.P,
+                        flushed ? U0S : nullptr, Sm1, n, npwx);
+      __syncthreads();
+      for (int s = tid; s < Sm1; s += nt) {
+        const ShiftRef sh{C, s, L.P};
+        for (int k = 0; k < kw; ++k) {
+          sh.at(L.o_xa, k) = zcd{0.0, 0.0};
+          sh.at(L.o_ub, k) = zcd{0.0, 0.0};
+        }
+        sh.at(L.o_scal, SC_UC) = zcd{1.0, 0.0};
+        sh.at(L.o_scal, SC_XD) = zcd{0.0, 0.0};
+      }
+      flushed = true;
+      kw = 0;
+      __syncthreads();
+    }
+    if (track) {
+      v_copy(W + (size_t)kw * npwx, RV(0), npwx);
+      v_copy(W + (size_t)(kw + 1) * npwx, UV(0), npwx);
+      for (int e = tid; e < 2 * (l + 1) * Db; e += nt) {
+        const int v = e / Db, q = e - v * Db;  // v <= l: cr, else cu
+        const double one = (v == 0 && q == 0) || (v == l + 1 && q == 1) ? 1.0 : 0.0;
+        (v <= l ? cr : cu)[e - (v <= l ? 0 : (l + 1) * Db)] = zcd{one, 0.0};
+      }
+      for (int s = tid; s < Sm1; s += nt) {
+        const ShiftRef sh{C, s, L.P};
+        for (int q = 0; q < L.D; ++q) {
+          sh.at(L.o_us, q) = zcd{q == Db ? 1.0 : 0.0, 0.0};
+          sh.at(L.o_xinc, q) = zcd{0.0, 0.0};
+        }
+      }
+    }
+    __syncthreads();
+
+    // ---- bicg_part (bicgstab.f90:520-702) ----
+    rho_old = -omega * rho_old;
+    for (int j = 0; j < l; ++j) {
+      const zcd rho = cta_dotu(RV(j), TR0, n, ss.red);
+      beta = alpha * rho / rho_old;
+      rho_old = rho;
+      {
+        const cplx<T> mb = ccast<T>(-beta);
+        for (int g = tid; g < n; g += nt)
+          for (int i = 0; i <= j; ++i) {
+            cplx<T> u = mb * UV(i)[g];
+            UV(i)[g] = u + RV(i)[g];
+          }
+        if (track)
+          for (int e = tid; e < (j + 1) * Db; e += nt) cu[e] = -beta * cu[e] + cr[e];
+      }
+      __syncthreads();
+      A.apply(UV(j), UV(j + 1), track ? W + (size_t)(kw + 2 + 2 * j) * npwx : nullptr, sigma_seed, sm, col);
+      if (track)
+        for (int q = tid; q < Db; q += nt) cu[(j + 1) * Db + q] = zcd{q == 2 + 2 * j ? 1.0 : 0.0, 0.0};
+      alpha = rho / cta_dotu(UV(j + 1), TR0, n, ss.red);
+      for (int s = tid; s < Sm1; s += nt) {
+        const ShiftRef sh{C, s, L.P};
+        shift_bicg_scalars(sh, L, alpha, beta, alpha_old);
+        if (track) replay_bicg1(sh, L, cr, j);
+      }
+      __syncthreads();
+      if (explicit_mode) {  // L15-L19 on the shift vectors, all shifts at once
+        for (long long e = tid; e < (long long)Sm1 * n; e += nt) {
+          const int s = (int)(e / n), g = (int)(e - (long long)s * n);
+          const cplx<T> mbs = ccast<T>(-SCAL(s, SC_BETA)), f = ccast<T>(SCAL(s, SC_F1));
+          for (int i = 0; i <= j; ++i) {
+            cplx<T> u = mbs * USV(s, i)[g];
+            USV(s, i)[g] = u + f * RV(i)[g];
+          }
+          XSV(s)[g] += ccast<T>(SCAL(s, SC_ALPHA)) * USV(s, 0)[g];
+          USV(s, j + 1)[g] = f * RV(j)[g];
+        }
+        __syncthreads();
+      }
+      alpha_old = alpha;
+      {
+        const cplx<T> ma = ccast<T>(-alpha);
+        for (int g = tid; g < n; g += nt)
+          for (int i = 0; i <= j; ++i) RV(i)[g] += ma * UV(i + 1)[g];
+        if (track)
+          for (int e = tid; e < (j + 1) * Db; e += nt) cr[e] += (-alpha) * cu[e + Db];
+      }
+      __syncthreads();
+      A.apply(RV(j), RV(j + 1), track ? W + (size_t)(kw + 3 + 2 * j) * npwx : nullptr, sigma_seed, sm, col);
+      if (track)
+        for (int q = tid; q < Db; q += nt) cr[(j + 1) * Db + q] = zcd{q == 3 + 2 * j ? 1.0 : 0.0, 0.0};
+      v_axpy(X, alpha, UV(0), n);
+      __syncthreads();
+      if (track)
+        for (int s = tid; s < Sm1; s += nt) replay_bicg2(ShiftRef{C, s, L.P}, L, cr, j);
+      if (explicit_mode)  // L26
+        for (long long e = tid; e < (long long)Sm1 * n; e += nt) {
+          const int s = (int)(e / n), g = (int)(e - (long long)s * n);
+          cplx<T> u = USV(s, j + 1)[g] + ccast<T>(SCAL(s, SC_F2)) * RV(j)[g];
+          u = ccast<T>(zcd{1.0, 0.0} / SCAL(s, SC_ALPHA)) * u;
+          USV(s, j + 1)[g] = u + ccast<T>(-SCAL(s, SC_SIG)) * USV(s, j)[g];
+        }
+      __syncthreads();
+    }
+    conv = sqrt(cta_nrm2sq(RV(0), n, ss.red)) < a.threshold;
+
+    if (!conv) {
+      // ---- mr_part (bicgstab.f90:708-931) ----
+      for (int jj = 1; jj <= l; ++jj) {
+        for (int ii = 1; ii <= jj - 1; ++ii) {
+          const zcd tau = cta_dotu(RV(jj), RV(ii), n, ss.red) / ss.nu[ii];
+          if (tid == 0) ss.tau[SGW_TAUIDX(jj, ii)] = tau;
+          v_axpy(RV(jj), -tau, RV(ii), n);
+          if (track)
+            for (int q = tid; q < Db; q += nt) cr[jj * Db + q] += (-tau) * cr[ii * Db + q];
+          __syncthreads();
+        }
+        const zcd nu = cta_dotu(RV(jj), RV(jj), n, ss.red);
+        const zcd gp = cta_dotu(RV(0), RV(jj), n, ss.red) / nu;
+        if (tid == 0) {
+          ss.nu[jj] = nu;
+          ss.gamma_p[jj] = gp;
+        }
+        __syncthreads();
+      }
+      if (tid == 0) {
+        ss.gamma[l] = ss.gamma_p[l];
+        for (int jj = l - 1; jj >= 1; --jj) {
+          zcd gsum = ss.gamma_p[jj];
+          for (int ii = jj + 1; ii <= l; ++ii) gsum = gsum - ss.tau[SGW_TAUIDX(ii, jj)] * ss.gamma[ii];
+          ss.gamma[jj] = gsum;
+        }
+        for (int jj = 1; jj <= l - 1; ++jj) {
+          zcd gsum = ss.gamma[jj + 1];
+          for (int ii = jj + 1; ii <= l - 1; ++ii) gsum = gsum + ss.tau[SGW_TAUIDX(ii, jj)] * ss.gamma[ii + 1];
+          ss.gamma_pp[jj] = gsum;
+        }
+      }
+      __syncthreads();
+      omega = ss.gamma[l];
+      for (int g = tid; g < n; g += nt) {  // L14-L17
+        cplx<T> x = X[g], u0 = UV(0)[g];
+        x += ccast<T>(ss.gamma[1]) * RV(0)[g];
+        u0 += ccast<T>(-ss.gamma[l]) * UV(l)[g];
+        for (int jj = 1; jj <= l - 1; ++jj) {
+          u0 += ccast<T>(-ss.gamma[jj]) * UV(jj)[g];
+          x += ccast<T>(ss.gamma_pp[jj]) * RV(jj)[g];
+        }
+        X[g] = x;
+        UV(0)[g] = u0;
+      }
+      for (int s = tid; s < Sm1; s += nt) {
+        const ShiftRef sh{C, s, L.P};
+        shift_mr_scalars(sh, L, ss);
+        if (track) replay_mr(sh, L, cr, ss);
+      }
+      __syncthreads();
+      if (explicit_mode) {  // L28-L34
+        for (long long e = tid; e < (long long)Sm1 * n; e += nt) {
+          const int s = (int)(e / n), g = (int)(e - (long long)s * n);
+          const ShiftRef sh{C, s, L.P};
+          cplx<T> x = XSV(s)[g], u0 = USV(s, 0)[g];
+          x += ccast<T>(sh.at(L.o_gpp, 0)) * RV(0)[g];
+          u0 += ccast<T>(-ss.gamma[l]) * USV(s, l)[g];
+          for (int jj = 1; jj <= l - 1; ++jj) {
+            u0 += ccast<T>(-ss.gamma[jj]) * USV(s, jj)[g];
+            x += ccast<T>(sh.at(L.o_gpp, jj)) * RV(jj)[g];
+          }
+          XSV(s)[g] = x;
+          USV(s, 0)[g] = ccast<T>(SCAL(s, SC_F1)) * u0;
+        }
+        __syncthreads();
+      }
+      for (int g = tid; g < n; g += nt) {  // delayed L32
+        cplx<T> r0 = RV(0)[g];
+        for (int jj = 1; jj <= l; ++jj) r0 += ccast<T>(-ss.gamma_p[jj]) * RV(jj)[g];
+        RV(0)[g] = r0;
+      }
+      __syncthreads();
+    }
+    if (track)
+      for (int s = tid; s < Sm1; s += nt) replay_window(ShiftRef{C, s, L.P}, L, kw);
+    if (track) kw += Db;
+    __syncthreads();
+    if (conv) break;
+    conv = sqrt(cta_nrm2sq(RV(0), n, ss.red)) < a.threshold;
+    if (conv) break;
+  }
+
+  // results: seed x, shifted x, bicgstab.f90:255-267
+  v_copy(xout, X, n);
+  if (track)
+    cta_basis_gemm<T>(xout + a.ldx, a.ldx, flushed, W, kw, C + L.o_xa, L.P, C + L.o_scal + SC_XD * L.P,
+                      flushed ? U0S : nullptr, Sm1, n, npwx);
+  if (explicit_mode)
+    for (long long e = tid; e < (long long)Sm1 * n; e += nt) {
+      const int s = (int)(e / n), g = (int)(e - (long long)s * n);
+      xout[(size_t)(s + 1) * a.ldx + g] = XSV(s)[g];
+    }
+  __syncthreads();
+  if (tid == 0) ss.flag = 0;
+  __syncthreads();
+  for (int e = tid; e < S * n; e += nt) {
+    const int s = e / n, g = e - s * n;
+    const cplx<T> v = xout[(size_t)s * a.ldx + g];
+    if (v.re != v.re || v.im != v.im) ss.flag = 1;
+  }
+  __syncthreads();
+  if (tid == 0) {
+    int ierr = iter > a.max_iter ? 1 : 0;
+    if (ss.flag) ierr = 2;
+    a.ierr[rhs] = ierr;
+    a.iters[rhs] = iter > a.max_iter ? a.max_iter : iter;
+  }
+  __syncthreads();
+#undef UV
+#undef RV
+#undef USV
+#undef XSV
+#undef SCAL
+}
+
+template <typename T, class ApplyT>
+__global__ void __launch_bounds__(kThreads, 1) msbicg_kernel(SolverArgs<T> a, ApplyT A) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ SeedShared ss;
+  __shared__ int s_rhs;
+  cplx<T>* sm = reinterpret_cast<cplx<T>*>(smem_raw);
+  cplx<T>* col = A.col_in_smem ? sm + A.smem_small() : a.col_global + (size_t)blockIdx.x * a.col_slot;
+  A.setup(sm);
+  while (true) {
+    if (threadIdx.x == 0) s_rhs = atomicAdd(a.counter, 1);
+    __syncthreads();
+    const int rhs = s_rhs;
+    __syncthreads();
+    if (rhs >= a.nrhs) break;
+    solve_one<T, ApplyT>(a, A, rhs, blockIdx.x, sm, col, ss);
+  }
+}
+
+}  // namespace sgw

@@ -1,0 +1,185 @@
+// The shifted Sternheimer operator A(sigma) = H + sigma + alpha_pv P_v applied by
+// one CTA to one vector (linear_op.f90:46-144, with QE h_psi for a
+// norm-conserving collinear insulator):
+//
+//   H psi(G) = |k+G|^2 psi(G)                                  kinetic (Ry)
+//            + fwfft[ V_loc(r) invfft[psi on the box] ](G)      local potential
+//            + sum_i beta_i(G) D_i <beta_i|psi>                 Kleinman-Bylander
+//   P_v psi  = sum_v evq_v <evq_v|psi>                         projector_psi :147-206
+//
+// The 3-D FFT is pruned to the G-sphere: the sphere occupies `ncol` columns
+// (i1, i2) of the box, so the i3 transforms run on those columns only
+// (compact `col` storage, ncol x ldz), and each i3-plane is expanded into a
+// padded nr2 x pitch plane in shared memory where the i2 transforms run only
+// on the i1 values that hold columns and the i1 transforms run on all rows.
+// V_loc(r) multiplies the plane between the inverse and forward transforms,
+// so the box never leaves the SM.  The CTA's threads split into NG groups that
+// work on different planes with their own named barriers (ids 1..NG).
+#pragma once
+#include "cplx.cuh"
+#include "fft.cuh"
+
+namespace sgw {
+
+template <typename T>
+struct PwView {
+  int npw, npwx;
+  int nr1, nr2, nr3, nnr;
+  int ncol, ni1;
+  int ldz;    // column pitch in `col` (odd, >= nr3)
+  int pitch;  // plane row pitch (odd, >= nr1)
+  const int* g_col;    // [npw] column of each sphere point
+  const int* g_i3;     // [npw] i3 of each sphere point
+  const int* col_pos;  // [ncol] i1 + pitch * i2
+  const int* i1_list;  // [ni1] i1 values holding columns
+  const T* g2kin;      // [npw]
+  const T* vrs;        // [nnr] V_loc(r), index i1 + nr1 (i2 + nr2 i3)
+  int nkb;
+  const cplx<T>* vkb;  // [nkb][npwx]
+  const T* dvan;       // [nkb]
+  int nocc;
+  const cplx<T>* evq;  // [nocc][npwx]
+  double alpha_pv;
+  FftPlan p1, p2, p3;
+  const cplx<T>* tw;   // [nr1 | nr2 | nr3] exp(+2 pi i e / n)
+};
+
+// Shared-memory elements (cplx<T>) the apply needs besides the column store.
+template <typename T>
+__host__ __device__ inline int pw_smem_small(const PwView<T>& op, int ng) {
+  return op.nr1 + op.nr2 + op.nr3 + op.nkb + op.nocc + ng * op.nr2 * op.pitch;
+}
+
+// CTA-wide sum of a double2 partial; result broadcast to every thread.
+__device__ __forceinline__ zcd cta_sum(zcd v, zcd* red) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    v.re += __shfl_xor_sync(0xffffffffu, v.re, o);
+    v.im += __shfl_xor_sync(0xffffffffu, v.im, o);
+  }
+  __syncthreads();  // red[] may still be read by a previous call
+  if (lane == 0) red[warp] = v;
+  __syncthreads();
+  zcd s = {0.0, 0.0};
+  for (int w = 0; w < nw; ++w) s += red[w];
+  return s;
+}
+
+// Unconjugated dot (ZDOTU) of two length-n vectors, CTA-wide, FP64 result.
+template <typename T>
+__device__ zcd cta_dotu(const cplx<T>* x, const cplx<T>* y, int n, zcd* red) {
+  cplx<T> p = {0, 0};
+  for (int i = threadIdx.x; i < n; i += blockDim.x) p += x[i] * y[i];
+  return cta_sum(ccast<double>(p), red);
+}
+
+// sum |x|^2 (for the 2-norm), CTA-wide
+template <typename T>
+__device__ double cta_nrm2sq(const cplx<T>* x, int n, zcd* red) {
+  T p = 0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) p += abs2(x[i]);
+  return cta_sum(zcd{(double)p, 0.0}, red).re;
+}
+
+// out = (H + sigma + alpha_pv P_v) in   (and out2 = the same, if non-null).
+// `sm` points at pw_smem_small() elements of shared memory; `col` at the
+// column store (ncol * ldz elements, shared or global).  Twiddles must already
+// sit at sm[0 .. nr1+nr2+nr3).
+template <typename T, int IPT>
+__device__ void pw_apply_cta(const PwView<T>& op, const int NG, const cplx<T>* __restrict__ in, cplx<T>* __restrict__ out,
+                             cplx<T>* __restrict__ out2, zcd sigma, cplx<T>* sm, cplx<T>* col) {
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const int lane = tid & 31, warp = tid >> 5, nwarp = nt >> 5;
+  const cplx<T>* tw1 = sm;
+  const cplx<T>* tw2 = sm + op.nr1;
+  const cplx<T>* tw3 = sm + op.nr1 + op.nr2;
+  cplx<T>* bec = sm + op.nr1 + op.nr2 + op.nr3;
+  cplx<T>* planes = bec + op.nkb + op.nocc;
+  const int nocc = (op.alpha_pv > 1e-14 || op.alpha_pv < -1e-14) ? op.nocc : 0;  // eps14, linear_op.f90:131
+
+  // <beta_i|psi> D_i and alpha_pv <evq_v|psi>, one warp per projection
+  for (int i = warp; i < op.nkb + nocc; i += nwarp) {
+    const cplx<T>* pr = (i < op.nkb) ? op.vkb + (size_t)i * op.npwx : op.evq + (size_t)(i - op.nkb) * op.npwx;
+    cplx<T> acc = {0, 0};
+    for (int g = lane; g < op.npw; g += 32) acc += cmul_conj_a(pr[g], in[g]);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      acc.re += __shfl_xor_sync(0xffffffffu, acc.re, o);
+      acc.im += __shfl_xor_sync(0xffffffffu, acc.im, o);
+    }
+    if (lane == 0) bec[i] = (i < op.nkb ? op.dvan[i] : (T)op.alpha_pv) * acc;
+  }
+  for (int e = tid; e < op.ncol * op.ldz; e += nt) col[e] = cplx<T>{0, 0};
+  __syncthreads();
+  for (int g = tid; g < op.npw; g += nt) col[op.g_col[g] * op.ldz + op.g_i3[g]] = in[g];
+  __syncthreads();
+  fft_lines<T, +1, IPT>(col, op.ncol, nullptr, op.ldz, 1, op.p3, tw3, tid, nt, 0);
+
+  // plane pass
+  {
+    const int gsize = nt / NG, g = tid / gsize, gtid = tid - g * gsize;
+    const int bar = (NG == 1) ? 0 : 1 + g;
+    cplx<T>* plane = planes + (size_t)g * op.nr2 * op.pitch;
+    const int psz = op.nr2 * op.pitch;
+    for (int i3 = g; i3 < op.nr3; i3 += NG) {
+      for (int e = gtid; e < psz; e += gsize) plane[e] = cplx<T>{0, 0};
+      group_sync(bar, gsize);
+      for (int c = gtid; c < op.ncol; c += gsize) plane[op.col_pos[c]] = col[c * op.ldz + i3];
+      group_sync(bar, gsize);
+      fft_lines<T, +1, IPT>(plane, op.ni1, op.i1_list, 0, op.pitch, op.p2, tw2, gtid, gsize, bar);
+      fft_lines<T, +1, IPT>(plane, op.nr2, nullptr, op.pitch, 1, op.p1, tw1, gtid, gsize, bar);
+      const T* v = op.vrs + (size_t)i3 * op.nr1 * op.nr2;
+      for (int e = gtid; e < op.nr1 * op.nr2; e += gsize) {
+        const int i2 = e / op.nr1, i1 = e - i2 * op.nr1;
+        plane[i2 * op.pitch + i1] = v[e] * plane[i2 * op.pitch + i1];
+      }
+      group_sync(bar, gsize);
+      fft_lines<T, -1, IPT>(plane, op.nr2, nullptr, op.pitch, 1, op.p1, tw1, gtid, gsize, bar);
+      fft_lines<T, -1, IPT>(plane, op.ni1, op.i1_list, 0, op.pitch, op.p2, tw2, gtid, gsize, bar);
+      for (int c = gtid; c < op.ncol; c += gsize) col[c * op.ldz + i3] = plane[op.col_pos[c]];
+      group_sync(bar, gsize);
+    }
+  }
+  __syncthreads();
+  fft_lines<T, -1, IPT>(col, op.ncol, nullptr, op.ldz, 1, op.p3, tw3, tid, nt, 0);
+
+  const T scale = (T)(1.0 / (double)op.nnr);
+  const cplx<T> sg = ccast<T>(sigma);
+  for (int g = tid; g < op.npw; g += nt) {
+    const cplx<T> x = in[g];
+    cplx<T> r = op.g2kin[g] * x + sg * x + scale * col[op.g_col[g] * op.ldz + op.g_i3[g]];
+    for (int i = 0; i < op.nkb; ++i) r += op.vkb[(size_t)i * op.npwx + g] * bec[i];
+    for (int v = 0; v < nocc; ++v) r += op.evq[(size_t)v * op.npwx + g] * bec[op.nkb + v];
+    out[g] = r;
+    if (out2) out2[g] = r;
+  }
+  __syncthreads();
+}
+
+// Dense operator A(sigma) x = A x + sigma x (the solver unit test's operator,
+// linear_problem.f90:100-113).  A is column-major n x n.
+template <typename T>
+struct DenseView {
+  int n, npwx;
+  const cplx<T>* a;
+};
+
+template <typename T>
+__device__ void dense_apply_cta(const DenseView<T>& op, const cplx<T>* __restrict__ in, cplx<T>* __restrict__ out,
+                                cplx<T>* __restrict__ out2, zcd sigma, cplx<T>* sm) {
+  for (int i = threadIdx.x; i < op.n; i += blockDim.x) sm[i] = in[i];
+  __syncthreads();
+  const cplx<T> sg = ccast<T>(sigma);
+  for (int row = threadIdx.x; row < op.n; row += blockDim.x) {
+    cplx<T> acc = {0, 0};
+    const cplx<T>* a = op.a + row;
+    for (int j = 0; j < op.n; ++j) acc += a[(size_t)j * op.n] * sm[j];
+    acc += sg * sm[row];
+    out[row] = acc;
+    if (out2) out2[row] = acc;
+  }
+  __syncthreads();
+}
+
+}  // namespace sgw

@@ -1,0 +1,238 @@
+"""Python mirror of SternheimerGW's linear-solver interface on the GB300 library.
+
+Reference interface (algo/linear_solver/src):
+  select_solver(config, AA, bb, sigma, xx, ierr)   select_solver.f90:67-161
+  bicgstab(config, AA, bb, sigma, xx, ierr)        bicgstab.f90:154-275
+  linear_solver(config, AA, bb, sigma, xx, ierr)   linear_solver.f90:82-194
+Here ``AA`` is an operator handle (PlaneWaveOperator or DenseOperator) because
+the GPU cannot call a host procedure; the functions return ``(xx, ierr)`` with
+xx of shape (n, num_shift) like the Fortran array.  ierr keeps the reference
+meaning: 0 converged, 1 not converged, 2 NaN, 3 complete basis.
+
+``solve_batch`` runs many right-hand sides in one persistent launch; it takes
+numpy arrays (host) or CUDA torch tensors (device, no copies).
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _capi
+
+BICGSTAB_MULTI = 1
+BICGSTAB_NO_MULTI = 2
+SGW_LINEAR_SOLVER = 3
+
+
+@dataclass
+class SelectSolverConfig:
+    """select_solver_type (select_solver.f90:48-62); defaults of gw_input.yml."""
+    priority: list = field(default_factory=lambda: [BICGSTAB_MULTI, SGW_LINEAR_SOLVER])
+    max_iter: int = 10000
+    threshold: float = 1e-4
+    bicg_lmax: int = 4
+
+    def to_c(self) -> _capi.SolverConfig:
+        if not self.priority:
+            raise ValueError("priority of the solvers not specified")
+        c = _capi.SolverConfig()
+        for i, p in enumerate(self.priority[:8]):
+            c.priority[i] = int(p)
+        c.num_priority = min(len(self.priority), 8)
+        c.max_iter = int(self.max_iter)
+        c.threshold = float(self.threshold)
+        c.bicg_lmax = int(self.bicg_lmax)
+        return c
+
+
+@dataclass
+class BicgstabConfig:
+    """bicgstab_type (bicgstab.f90:44-55)."""
+    lmax: int = 4
+    threshold: float = 1e-4
+    max_iter: int = 10000
+
+
+@dataclass
+class LinearSolverConfig:
+    """linear_solver_config (linear_solver.f90:41-58)."""
+    threshold: float = 1e-4
+    max_iter: int = 10000
+
+
+def _c128(a):
+    return np.ascontiguousarray(a, dtype=np.complex128)
+
+
+def _p(a):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+class _Operator:
+    handle: C.c_void_p
+    n: int
+
+    def close(self):
+        if getattr(self, "handle", None):
+            _capi.lib().sgw_operator_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_alpha_pv(self, alpha_pv: float):
+        _capi.check(_capi.lib().sgw_operator_set_alpha_pv(self.handle, float(alpha_pv)), "sgw_operator_set_alpha_pv")
+
+    def apply(self, sigma, x):
+        """A(sigma) x for x of shape (n,) or (n, m) (the reference's AA)."""
+        x = np.asarray(x, dtype=np.complex128)
+        one = x.ndim == 1
+        xm = np.asfortranarray(x.reshape(self.n, -1))
+        out = np.zeros_like(xm, order="F")
+        _capi.check(_capi.lib().sgw_operator_apply(self.handle, _capi.ZComplex(complex(sigma).real, complex(sigma).imag),
+                                                   xm.shape[1], _p(xm), self.n, _p(out), self.n), "sgw_operator_apply")
+        return out[:, 0] if one else out
+
+    def last_timing(self):
+        ms = C.c_double(0)
+        n = C.c_int64(0)
+        _capi.check(_capi.lib().sgw_last_timing(self.handle, C.byref(ms), C.byref(n)), "sgw_last_timing")
+        return ms.value, n.value
+
+
+class DenseOperator(_Operator):
+    """A(sigma) x = A x + sigma x (linear_problem.f90:100-113)."""
+
+    def __init__(self, a):
+        a = np.asfortranarray(a, dtype=np.complex128)
+        self.n = a.shape[0]
+        h = C.c_void_p()
+        _capi.check(_capi.lib().sgw_operator_create_dense(self.n, _p(a), self.n, C.byref(h)), "sgw_operator_create_dense")
+        self.handle = h
+
+
+class PlaneWaveOperator(_Operator):
+    """(H + sigma + alpha_pv P_v) on the k+q G-sphere (linear_op.f90:46-206).
+
+    ``system`` is a dict as produced by :mod:`sternheimergw_gb300.synth`
+    (npw, nr, nl, g2kin, vrs, vkb, dvan, evq, alpha_pv).
+    """
+
+    def __init__(self, system, alpha_pv=None):
+        s = system
+        self.n = int(s["npw"])
+        self._keep = dict(
+            nl=np.ascontiguousarray(s["nl"], dtype=np.int32),
+            g2kin=np.ascontiguousarray(s["g2kin"], dtype=np.float64),
+            vrs=np.ascontiguousarray(s["vrs"], dtype=np.float64),
+            vkb=np.asfortranarray(s["vkb"], dtype=np.complex128),
+            dvan=np.ascontiguousarray(s["dvan"], dtype=np.float64),
+            evq=np.asfortranarray(s["evq"], dtype=np.complex128),
+        )
+        k = self._keep
+        d = _capi.PwOperatorDesc()
+        d.npw = self.n
+        d.npwx = self.n
+        d.nr1, d.nr2, d.nr3 = [int(v) for v in s["nr"]]
+        d.nl = k["nl"].ctypes.data
+        d.g2kin = k["g2kin"].ctypes.data
+        d.vrs = k["vrs"].ctypes.data
+        d.nkb = k["vkb"].shape[1]
+        d.vkb = k["vkb"].ctypes.data
+        d.dvan = k["dvan"].ctypes.data
+        d.nbnd_occ = k["evq"].shape[1]
+        d.evq = k["evq"].ctypes.data
+        d.alpha_pv = float(s["alpha_pv"] if alpha_pv is None else alpha_pv)
+        self.alpha_pv = d.alpha_pv
+        h = C.c_void_p()
+        _capi.check(_capi.lib().sgw_operator_create_pw(C.byref(d), C.byref(h)), "sgw_operator_create_pw")
+        self.handle = h
+
+
+def bicgstab(config: BicgstabConfig, AA: _Operator, bb, sigma):
+    """bicgstab.f90:154-275 -> (xx[n, S], ierr)."""
+    bb = _c128(bb)
+    sigma = _c128(np.atleast_1d(sigma))
+    xx = np.zeros((sigma.size, AA.n), dtype=np.complex128)
+    ierr = C.c_int32(0)
+    _capi.check(_capi.lib().sgw_bicgstab(AA.handle, config.lmax, config.threshold, config.max_iter, _p(bb), bb.size,
+                                         _p(sigma), sigma.size, _p(xx), AA.n, C.byref(ierr)), "sgw_bicgstab")
+    return xx.T.copy(), ierr.value
+
+
+def linear_solver(config: LinearSolverConfig, AA: _Operator, bb, sigma):
+    """linear_solver.f90:82-194 -> (xx[n, S], ierr)."""
+    bb = _c128(bb)
+    sigma = _c128(np.atleast_1d(sigma))
+    xx = np.zeros((sigma.size, AA.n), dtype=np.complex128)
+    ierr = C.c_int32(0)
+    _capi.check(_capi.lib().sgw_linear_solver(AA.handle, config.threshold, config.max_iter, _p(bb), bb.size, _p(sigma),
+                                              sigma.size, _p(xx), AA.n, C.byref(ierr)), "sgw_linear_solver")
+    return xx.T.copy(), ierr.value
+
+
+def select_solver(config: SelectSolverConfig, AA: _Operator, bb, sigma):
+    """select_solver.f90:67-161 -> (xx[n, S], ierr)."""
+    bb = _c128(bb)
+    sigma = _c128(np.atleast_1d(sigma))
+    xx = np.zeros((sigma.size, AA.n), dtype=np.complex128)
+    ierr = C.c_int32(0)
+    cfg = config.to_c()
+    _capi.check(_capi.lib().sgw_select_solver(AA.handle, C.byref(cfg), _p(bb), bb.size, _p(sigma), sigma.size, _p(xx),
+                                              AA.n, C.byref(ierr)), "sgw_select_solver")
+    return xx.T.copy(), ierr.value
+
+
+def _is_torch(x):
+    return type(x).__module__.startswith("torch")
+
+
+def solve_batch(AA: _Operator, bb, sigma, *, lmax=4, threshold=1e-4, max_iter=10000, precision=0, history_iters=0,
+                refine_max=0, refine_threshold=0.0, out=None):
+    """Multishift solve of nrhs right-hand sides sharing one operator.
+
+    bb: (nrhs, n) complex128; sigma: (nrhs, S) complex128.  numpy arrays run
+    through host memory (copies inside the call); CUDA torch tensors stay on
+    the device.  Returns (xx[nrhs, S, n], ierr[nrhs], iters[nrhs]).
+    """
+    d = _capi.BatchDesc()
+    if _is_torch(bb):
+        import torch
+        assert bb.is_cuda and sigma.is_cuda and bb.dtype == torch.complex128 and sigma.dtype == torch.complex128
+        bb = bb.contiguous()
+        sigma = sigma.contiguous()
+        nrhs, n = bb.shape
+        S = sigma.shape[1]
+        xx = out if out is not None else torch.empty((nrhs, S, n), dtype=torch.complex128, device=bb.device)
+        ierr = torch.zeros(nrhs, dtype=torch.int32, device=bb.device)
+        iters = torch.zeros(nrhs, dtype=torch.int32, device=bb.device)
+        d.memory = 1
+        d.bb, d.sigma, d.xx = bb.data_ptr(), sigma.data_ptr(), xx.data_ptr()
+        d.ierr, d.iters = ierr.data_ptr(), iters.data_ptr()
+    else:
+        bb = _c128(bb)
+        sigma = _c128(sigma)
+        nrhs, n = bb.shape
+        S = sigma.shape[1]
+        xx = out if out is not None else np.zeros((nrhs, S, n), dtype=np.complex128)
+        ierr = np.zeros(nrhs, dtype=np.int32)
+        iters = np.zeros(nrhs, dtype=np.int32)
+        d.memory = 0
+        d.bb, d.sigma, d.xx = bb.ctypes.data, sigma.ctypes.data, xx.ctypes.data
+        d.ierr, d.iters = ierr.ctypes.data, iters.ctypes.data
+    if n != AA.n:
+        raise ValueError("right-hand side and operator sizes differ")
+    d.nrhs, d.num_shift, d.lmax, d.max_iter = nrhs, S, int(lmax), int(max_iter)
+    d.threshold = float(threshold)
+    d.precision = int(precision)
+    d.history_iters = int(history_iters)
+    d.refine_max = int(refine_max)
+    d.refine_threshold = float(refine_threshold)
+    d.ldb, d.lds, d.ldx, d.ldr = n, S, n, S * n
+    _capi.check(_capi.lib().sgw_solve_batch(AA.handle, C.byref(d)), "sgw_solve_batch")
+    return xx, ierr, iters

@@ -1,0 +1,29 @@
+"""The C ABI: the in-tree library loads and exports every declared entry point
+(no compute call, so this runs without a GPU)."""
+import ctypes
+import os
+import re
+
+from conftest import ROOT
+
+
+def declared_functions():
+    text = open(os.path.join(ROOT, "include", "sgw_capi.h")).read()
+    return sorted(set(re.findall(r"^(?:sgw_status|const char\*)\s+(sgw_\w+)\s*\(", text, re.M)))
+
+
+def test_header_declares_entry_points():
+    names = declared_functions()
+    for n in ("sgw_select_solver", "sgw_bicgstab", "sgw_linear_solver", "sgw_operator_create_pw",
+              "sgw_solve_batch", "sgw_operator_destroy"):
+        assert n in names
+
+
+def test_library_exports_every_declared_symbol():
+    from sternheimergw_gb300 import _capi
+    lib = _capi.lib()
+    for name in declared_functions():
+        assert hasattr(lib, name), name
+    bound = {n for n, _, _ in _capi.SIGNATURES}
+    assert set(declared_functions()) <= bound
+    assert lib.sgw_version().startswith(b"sgw_gb300")
