@@ -152,6 +152,22 @@ typedef struct sgw_batch_desc {
 
 sgw_status sgw_solve_batch(sgw_operator* op, const sgw_batch_desc* desc);
 
+/* Size of the fixed device scratch array used by sgw_solve_batch_noalloc. */
+#define SGW_NOALLOC_SCRATCH_BYTES (32u * 1024u * 1024u)
+
+/* sgw_solve_batch without any device allocation, for callers that cannot call
+ * cudaMalloc while they solve (code inside a captured stream, memory-capped or
+ * pool-managed processes, host codes whose device budget is fixed up front).
+ * No counterpart in the reference, whose solver allocates its Krylov arrays on
+ * every call (bicgstab.f90:304-490).  FP64 only (precision = 0), device
+ * pointers only (memory = 1); iters may be null.  All scratch comes from one
+ * static device array of SGW_NOALLOC_SCRATCH_BYTES that every GPU loading the
+ * library holds until exit; problems needing more scratch per right-hand side
+ * are rejected with SGW_ERR_UNSUPPORTED.  Calls share that array: calls that
+ * overlap on the GPU race.  The first call on a device looks the array up
+ * (cudaGetSymbolAddress); make it before any stream capture. */
+sgw_status sgw_solve_batch_noalloc(sgw_operator* op, const sgw_batch_desc* desc);
+
 /* Device time (ms) of the last solve on this handle's stream, measured with
  * CUDA events around the kernels; and the number of kernel launches it used. */
 sgw_status sgw_last_timing(sgw_operator* op, double* ms, int64_t* launches);

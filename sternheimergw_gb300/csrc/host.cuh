@@ -135,4 +135,6 @@ template <typename T> sgw_status run_sgw(sgw_operator* op, const SgwArgs<T>& a);
 template <typename T>
 sgw_status run_apply(sgw_operator* op, int m, const cplx<T>* x, long long ldi, cplx<T>* ax, long long ldo, zcd sigma);
 sgw_status solve_mixed(sgw_operator* op, const BatchDev& b, int refine_max, double refine_thr);
+template <typename T>
+sgw_status run_msbicg_in(sgw_operator* op, const BatchDev& b, unsigned char* region, size_t region_bytes);
 }  // namespace sgw

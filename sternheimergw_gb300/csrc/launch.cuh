@@ -123,3 +123,84 @@ sgw_status run_apply(sgw_operator* op, int m, const cplx<T>* x, long long ldi, c
 }
 
 }  // namespace sgw
+
+namespace sgw {
+
+// The multishift solve with every scratch buffer carved from one caller-given
+// device region (no allocation).  Layout: [work counter | per-CTA vector slots |
+// per-CTA coefficient slots | per-CTA column stores | iteration counts].  The
+// history window and the CTA count shrink until the layout fits; a problem
+// whose single slot does not fit returns SGW_ERR_UNSUPPORTED.
+template <typename T>
+sgw_status run_msbicg_in(sgw_operator* op, const BatchDev& b, unsigned char* region, size_t region_bytes) {
+  const int n = op->n, npwx = op->npwx, l = b.lmax, Sm1 = b.nshift - 1;
+  const int Db = 2 * l + 2;
+  const int P = std::max(32, (Sm1 + 31) / 32 * 32);
+  const int mode = l > 8 ? 1 : 0;
+  const long long colsz = (op->kind == 1 && !pwshape<T>(op).col_in_smem) ? col_elems<T>(op) : 0;
+  auto align = [](size_t v) { return (v + 255) / 256 * 256; };
+  const size_t head = 256;
+  const size_t iters_bytes = b.iters ? 0 : align(sizeof(int) * (size_t)b.nrhs);
+  int Tw = b.history_iters > 0 ? std::min(b.history_iters, b.max_iter) : std::min(8, b.max_iter);
+  for (; Tw >= 1; --Tw) {
+    const int Kcap = (Sm1 > 0 && mode == 0) ? Db * Tw : 0;
+    const long long nvec_slot = (2LL * l + 4) + (mode == 0 ? Kcap + (Sm1 > 0 ? Sm1 : 0) : (long long)Sm1 * (l + 2));
+    const CoefLayout L(l, P, Kcap);
+    const size_t vec_b = align((size_t)nvec_slot * npwx * sizeof(cplx<T>));
+    const size_t coef_b = align((size_t)L.total * sizeof(zcd));
+    const size_t col_b = align((size_t)colsz * sizeof(cplx<T>));
+    const size_t per_slot = vec_b + coef_b + col_b;
+    if (head + iters_bytes + per_slot > region_bytes) {
+      if (mode == 1 || Sm1 == 0) break;  // the window does not change the slot size
+      continue;
+    }
+    const int fit = (int)std::min<size_t>((region_bytes - head - iters_bytes) / per_slot, (size_t)1 << 20);
+    const int nslots = std::max(1, std::min(std::min(b.nrhs, op->num_sms), fit));
+    unsigned char* p = region + head;
+    SolverArgs<T> a{};
+    a.counter = reinterpret_cast<int*>(region);
+    a.ws_vec = reinterpret_cast<cplx<T>*>(p);
+    p += (size_t)nslots * vec_b;
+    a.ws_coef = reinterpret_cast<zcd*>(p);
+    p += (size_t)nslots * coef_b;
+    a.col_global = reinterpret_cast<cplx<T>*>(p);
+    p += (size_t)nslots * col_b;
+    a.iters = b.iters ? b.iters : reinterpret_cast<int*>(p);
+    a.lmax = l;
+    a.max_iter = b.max_iter;
+    a.threshold = b.threshold;
+    a.nshift = b.nshift;
+    a.nrhs = b.nrhs;
+    a.npw = n;
+    a.npwx = npwx;
+    a.bb = reinterpret_cast<const cplx<T>*>(b.bb);
+    a.ldb = b.ldb;
+    a.sigma = b.sigma;
+    a.lds = b.lds;
+    a.xx = reinterpret_cast<cplx<T>*>(b.xx);
+    a.ldx = b.ldx;
+    a.ldr = b.ldr;
+    a.ierr = b.ierr;
+    a.nvec_slot = (long long)(vec_b / (sizeof(cplx<T>) * npwx));
+    a.ncoef_slot = (long long)(coef_b / sizeof(zcd));
+    a.Kcap = Kcap;
+    a.P = P;
+    a.col_slot = (long long)(col_b / sizeof(cplx<T>));
+    a.mode = mode;
+    // the region keeps the previous call's contents: the work counter must start at zero
+    SGW_CK(cudaMemsetAsync(region, 0, sizeof(int), op->stream));
+    return with_applier<T>(op, [&](auto A, size_t smem) -> sgw_status {
+      auto kern = msbicg_kernel<T, decltype(A)>;
+      SGW_CK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      kern<<<nslots, kThreads, smem, op->stream>>>(a, A);
+      SGW_CK(cudaGetLastError());
+      op->last_launches += 1;
+      return SGW_OK;
+    });
+  }
+  set_error("problem needs more scratch per right-hand side than the fixed no-allocation region of " +
+            std::to_string(region_bytes) + " bytes");
+  return SGW_ERR_UNSUPPORTED;
+}
+
+}  // namespace sgw
