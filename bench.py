@@ -206,6 +206,73 @@ def run_reference(args, rank, world):
     print(json.dumps(out), flush=True)
 
 
+def fp32_peak_tflops():
+    """Measured FP32 (CUDA-core) throughput: cuBLAS SGEMM 8192^3 with TF32 off, best of 5."""
+    import torch
+    prev = torch.backends.cuda.matmul.allow_tf32
+    torch.backends.cuda.matmul.allow_tf32 = False
+    a = torch.randn(8192, 8192, dtype=torch.float32, device="cuda")
+    b = torch.randn(8192, 8192, dtype=torch.float32, device="cuda")
+    torch.matmul(a, b)
+    torch.cuda.synchronize()
+    best = 1e9
+    for _ in range(5):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b)
+        e1.record()
+        torch.cuda.synchronize()
+        best = min(best, e0.elapsed_time(e1))
+    torch.backends.cuda.matmul.allow_tf32 = prev
+    del a, b
+    return 2.0 * 8192 ** 3 / (best * 1e-3) / 1e12
+
+
+def time_path(op, bb_d, sg_d, x_d, precision, warmup, steps, l2, name):
+    """Warm-up then timed steps of one precision; device times from the library's CUDA events."""
+    import sternheimergw_gb300 as sg
+    for w in range(warmup):
+        flush_l2(l2)
+        sg.solve_batch(op, bb_d, sg_d, lmax=LMAX, threshold=THRESHOLD, precision=precision, out=x_d)
+        log(f"[bench] {name} warmup {w}: {op.last_timing()[0]:.1f} ms")
+    dev_ms, launches, kern = [], 0, {0: [0.0, 0], 1: [0.0, 0], 2: [0.0, 0]}
+    iters = ierr = None
+    for k in range(steps):
+        flush_l2(l2)
+        _, ierr, iters = sg.solve_batch(op, bb_d, sg_d, lmax=LMAX, threshold=THRESHOLD, precision=precision, out=x_d)
+        ms, nl = op.last_timing()
+        dev_ms.append(ms)
+        launches += nl
+        for kk in kern:
+            km, kn = op.kernel_timing(kk)
+            kern[kk][0] += km
+            kern[kk][1] += kn
+        it = iters.cpu().numpy()
+        log(f"[bench] {name} step {k}: {ms:.1f} ms, ierr max {int(ierr.max())}, iters {it.min()}..{it.max()}")
+    return dict(ms=float(np.mean(dev_ms)), launches=launches, kern=kern, iters=iters.cpu().numpy(),
+                ierr=ierr.cpu().numpy())
+
+
+def w_error(s, f, bb, x64_d, xm_d):
+    """Relative error of W(G, G'; omega) (all perturbation pairs, every frequency) of the mixed
+    solve against the FP64 solve, normwise per frequency and elementwise."""
+    import torch
+    from sternheimergw_gb300 import linter
+    npert, nocc = len(s["gpert"]), s["nocc"]
+    S = x64_d.shape[1]
+    B = torch.from_numpy(bb.reshape(npert, nocc, -1)).cuda()
+    v = linter.coulomb_v(s)
+    W = []
+    for x in (x64_d, xm_d):
+        chi = linter.chi_matrix(B, x.view(npert, nocc, S, -1), f)
+        W.append(linter.w_from_chi(chi, v))
+    d = W[1] - W[0]
+    norm = (torch.linalg.matrix_norm(d) / torch.linalg.matrix_norm(W[0])).max().item()
+    big = W[0].abs() >= 1e-3 * W[0].abs().amax(dim=(1, 2), keepdim=True)
+    elem = (d.abs() / W[0].abs())[big].max().item()
+    return norm, elem
+
+
 def run_gpu(args, rank, world):
     import torch
     import torch.distributed as dist
@@ -222,7 +289,8 @@ def run_gpu(args, rank, world):
     op = sg.PlaneWaveOperator(s)
     bb_d = torch.from_numpy(bb).cuda()
     sg_d = torch.from_numpy(sigma).cuda()
-    x_d = torch.empty((nrhs, S, n), dtype=torch.complex128, device="cuda")
+    x64_d = torch.empty((nrhs, S, n), dtype=torch.complex128, device="cuda")
+    xm_d = torch.empty((nrhs, S, n), dtype=torch.complex128, device="cuda")
     l2 = torch.zeros(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MB > L2
 
     def barrier():
@@ -230,36 +298,24 @@ def run_gpu(args, rank, world):
         if world > 1:
             dist.barrier()
 
-    precision = 0
-    for w in range(args.warmup):
-        flush_l2(l2)
-        _, ierr, iters = sg.solve_batch(op, bb_d, sg_d, lmax=LMAX, threshold=THRESHOLD, precision=precision, out=x_d)
-        ms, _ = op.last_timing()
-        log(f"[bench] warmup {w}: {ms:.1f} ms")
     barrier()
-    dev_ms, launches, iters_all = [], 0, None
     with ClockSampler(dev) as clk:
         t0 = time.time()
-        for k in range(args.steps):
-            flush_l2(l2)
-            _, ierr, iters = sg.solve_batch(op, bb_d, sg_d, lmax=LMAX, threshold=THRESHOLD, precision=precision,
-                                             out=x_d)
-            ms, nl = op.last_timing()
-            dev_ms.append(ms)
-            launches += nl
-            iters_all = iters.cpu().numpy()
-            log(f"[bench] step {k}: {ms:.1f} ms, ierr max {int(ierr.max())}, iters {iters_all.min()}..{iters_all.max()}")
+        p64 = time_path(op, bb_d, sg_d, x64_d, 0, args.warmup, args.steps, l2, "fp64")
+        pm = time_path(op, bb_d, sg_d, xm_d, 1, args.warmup, args.steps, l2, "mixed")
         barrier()
         wall = time.time() - t0
-    ms_step = float(np.mean(dev_ms))
+    ms_m, ms_64 = pm["ms"], p64["ms"]
     if world > 1:
-        t = torch.tensor([ms_step], device="cuda")
+        t = torch.tensor([ms_m, ms_64], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_step = float(t.item())
+        ms_m, ms_64 = float(t[0].item()), float(t[1].item())
     solves = nrhs * S
-    value = world * solves / (ms_step * 1e-3)
+    value = world * solves / (ms_m * 1e-3)
+    value64 = world * solves / (ms_64 * 1e-3)
+    w_norm, w_elem = w_error(s, f, bb, x64_d, xm_d)
 
-    # end to end through the C ABI with pinned host buffers
+    # end to end through the C ABI with pinned host buffers (mixed precision, the headline path)
     bb_h = torch.from_numpy(bb).pin_memory()
     sg_h = torch.from_numpy(sigma).pin_memory()
     x_h = torch.empty((nrhs, S, n), dtype=torch.complex128).pin_memory()
@@ -268,8 +324,7 @@ def run_gpu(args, rank, world):
         flush_l2(l2)
         torch.cuda.synchronize()
         t = time.time()
-        sg.solve_batch(op, bb_h.numpy(), sg_h.numpy(), lmax=LMAX, threshold=THRESHOLD, precision=precision,
-                       out=x_h.numpy())
+        sg.solve_batch(op, bb_h.numpy(), sg_h.numpy(), lmax=LMAX, threshold=THRESHOLD, precision=1, out=x_h.numpy())
         e2e_ms.append((time.time() - t) * 1e3)
     e2e_value = world * solves / (float(np.median(e2e_ms)) * 1e-3)
     h2d = bb.nbytes + sigma.nbytes
@@ -277,37 +332,51 @@ def run_gpu(args, rank, world):
 
     out = None
     if rank == 0:
-        peak = fp64_peak_tflops()
-        flops = step_flops(s, iters_all, S)
-        achieved = flops / (ms_step * 1e-3) / 1e12
+        peak64 = fp64_peak_tflops()
+        peak32 = fp32_peak_tflops()
+        k64_ms, k64_n = p64["kern"][0]
+        f64 = step_flops(s, p64["iters"], S)
+        ach64 = f64 / (k64_ms / max(k64_n, 1) * 1e-3) / 1e12
+        k32_ms, k32_n = pm["kern"][1]
+        kres_ms, kres_n = pm["kern"][2]
+        f32 = step_flops(s, pm["iters"], S) * args.steps  # FP32 iterations of all rounds, all timed steps
+        ach32 = f32 / (k32_ms * 1e-3) / 1e12
         sample = min(nrhs, 32 * (os.cpu_count() or 1))
         cpu_v, cpu_dt, _ = cpu_reference(s, bb, sigma, sample, os.cpu_count() or 1)
-        peaks = {}
-        try:
-            peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
-        except OSError:
-            pass
         out = {
             "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "c128", "data": "synthetic",
+            "warmup": args.warmup, "ms_per_step": ms_m, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "c64 Krylov + fp64 refinement", "data": "synthetic",
             "config": {"workload": WORKLOAD, "rhs_per_step": nrhs, "shifts": S, "solves_per_step": solves,
-                       "precision": "fp64", "l2": "256 MB buffer written between steps; outputs 4.6 GB > L2",
-                       "mean_outer_iterations": float(np.mean(iters_all))},
+                       "precision": "mixed (headline) and fp64", "refine_target": 1e-9,
+                       "l2": "256 MB buffer written between steps; outputs 4.6 GB > L2",
+                       "mean_fp32_iterations": float(np.mean(pm["iters"])),
+                       "mean_fp64_iterations": float(np.mean(p64["iters"]))},
+            "plain_fp64": {"value": value64, "unit": "solves/s", "ms_per_step": ms_64,
+                           "ierr_max": int(p64["ierr"].max())},
+            "speedup_mixed_vs_fp64": value / value64,
+            "w_err": {"normwise_max_over_freq": w_norm, "elementwise_max": w_elem,
+                      "elements": "W(G,G';omega) over 113x113 perturbations x 35 frequencies, |W|>=1e-3 max",
+                      "ok": bool(w_norm <= 1e-6), "mixed_ierr_max": int(pm["ierr"].max())},
             "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h), "ms_per_step": float(np.median(e2e_ms))},
-            "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                         "frac": achieved / peak, "traffic": None,
-                         "peak_source": "in-run cuBLAS DGEMM 8192^3 (MEASURED_PEAKS.json has no FP64 figure)",
-                         "kernel": "msbicg_kernel (one launch per step)", "flops_per_launch": flops},
+            "roofline": {"bound": "fp32", "achieved": ach32, "peak": peak32, "unit": "TFLOP/s",
+                         "frac": ach32 / peak32, "traffic": None,
+                         "kernel": "msbicg_kernel<float> (mixed rounds)",
+                         "launches_per_step": k32_n / args.steps, "ms_per_launch": k32_ms / max(k32_n, 1),
+                         "peak_source": "in-run cuBLAS SGEMM 8192^3, TF32 off"},
+            "roofline_fp64": {"bound": "fp64", "achieved": ach64, "peak": peak64, "unit": "TFLOP/s",
+                              "frac": ach64 / peak64, "traffic": None, "kernel": "msbicg_kernel<double>",
+                              "ms_per_launch": k64_ms / max(k64_n, 1), "flops_per_launch": f64,
+                              "peak_source": "in-run cuBLAS DGEMM 8192^3 (MEASURED_PEAKS.json has no FP64 figure)"},
+            "mixed_kernel_ms_per_step": {"fp32_solve": k32_ms / args.steps, "fp64_seed_residual": kres_ms / args.steps,
+                                         "total": ms_m},
             "cpu_baseline": {"value": cpu_v, "unit": "solves/s", "cores": os.cpu_count() or 1, "kind": "port",
                              "sample": f"{sample} of {nrhs} right-hand sides x {S} shifts, {cpu_dt:.1f}s"},
-            "gpu_launches": int(launches),
+            "gpu_launches": int(pm["launches"]),
             "clocks": clk.summary(),
             "wall_s_timed": wall,
         }
-        if peaks.get("hbm_gbs"):
-            out["roofline"]["hbm_peak_gbs"] = peaks["hbm_gbs"]
         print(json.dumps(out), flush=True)
     return out
 

@@ -172,6 +172,12 @@ sgw_status sgw_solve_batch_noalloc(sgw_operator* op, const sgw_batch_desc* desc)
  * CUDA events around the kernels; and the number of kernel launches it used. */
 sgw_status sgw_last_timing(sgw_operator* op, double* ms, int64_t* launches);
 
+/* Device time (ms, CUDA events on the handle's stream) and launch count of
+ * one kernel in the last sgw_solve_batch call: kernel 0 = FP64 multishift
+ * solve, 1 = FP32 multishift solve (mixed precision), 2 = FP64 seed residual
+ * (mixed precision). */
+sgw_status sgw_kernel_timing(sgw_operator* op, int32_t kernel, double* ms, int64_t* launches);
+
 /* One-line description of the last error on this thread. */
 const char* sgw_last_error(void);
 

@@ -54,6 +54,7 @@ SIGNATURES = [
     ("sgw_solve_batch", C.c_int, [C.c_void_p, C.POINTER(BatchDesc)]),
     ("sgw_solve_batch_noalloc", C.c_int, [C.c_void_p, C.POINTER(BatchDesc)]),
     ("sgw_last_timing", C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_int64)]),
+    ("sgw_kernel_timing", C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_int64)]),
     ("sgw_last_error", C.c_char_p, []),
     ("sgw_version", C.c_char_p, []),
 ]

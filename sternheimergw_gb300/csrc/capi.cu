@@ -96,7 +96,24 @@ static sgw_status init_common(sgw_operator* op) {
   SGW_CK(cudaStreamCreateWithFlags(&op->stream, cudaStreamNonBlocking));
   SGW_CK(cudaEventCreate(&op->ev0));
   SGW_CK(cudaEventCreate(&op->ev1));
+  for (int i = 0; i < 2 * kMaxTimedLaunches; ++i) SGW_CK(cudaEventCreate(&op->kev[i]));
   return SGW_OK;
+}
+
+// Sum the per-kernel event pairs of the finished solve (stream already synchronised).
+static void collect_kernel_times(sgw_operator* op) {
+  for (int k = 0; k < K_NUM; ++k) {
+    op->kernel_ms[k] = 0.0;
+    op->kernel_launches[k] = 0;
+  }
+  for (int i = 0; i < op->kev_used; ++i) {
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, op->kev[2 * i], op->kev[2 * i + 1]) == cudaSuccess) {
+      op->kernel_ms[op->kev_kind[i]] += ms;
+      op->kernel_launches[op->kev_kind[i]] += 1;
+    }
+  }
+  op->kev_used = 0;
 }
 
 template <typename T>
@@ -300,6 +317,7 @@ static sgw_status solve_batch(sgw_operator* op, const sgw_batch_desc* d) {
   sgw_status s = check_batch(op, d);
   if (s != SGW_OK) return s;
   op->last_launches = 0;
+  op->kev_used = 0;
   BatchDev b{d->nrhs, d->num_shift, d->lmax, d->max_iter, d->history_iters, d->threshold, nullptr, 0, nullptr, 0,
              nullptr, 0, 0, nullptr, nullptr};
   const int n = op->n, S = d->num_shift, R = d->nrhs;
@@ -355,6 +373,7 @@ static sgw_status solve_batch(sgw_operator* op, const sgw_batch_desc* d) {
   float ms = 0.f;
   SGW_CK(cudaEventElapsedTime(&ms, op->ev0, op->ev1));
   op->last_ms = ms;
+  collect_kernel_times(op);
   return SGW_OK;
 }
 
@@ -492,6 +511,8 @@ sgw_status sgw_operator_destroy(sgw_operator* op) {
                     &op->ws32.vec, &op->ws32.coef, &op->ws32.col, &op->ws32.counter, &op->st_bb, &op->st_sigma,
                     &op->st_xx, &op->st_ierr, &op->st_iters, &op->st_misc, &op->st_misc2, &op->st_misc3};
   for (DevBuf* b : bufs) b->release();
+  for (int i = 0; i < 2 * kMaxTimedLaunches; ++i)
+    if (op->kev[i]) cudaEventDestroy(op->kev[i]);
   if (op->ev0) cudaEventDestroy(op->ev0);
   if (op->ev1) cudaEventDestroy(op->ev1);
   if (op->stream) cudaStreamDestroy(op->stream);
@@ -585,6 +606,13 @@ sgw_status sgw_last_timing(sgw_operator* op, double* ms, int64_t* launches) {
   if (!op) return arg_error("null operator");
   if (ms) *ms = op->last_ms;
   if (launches) *launches = op->last_launches;
+  return SGW_OK;
+}
+
+sgw_status sgw_kernel_timing(sgw_operator* op, int32_t kernel, double* ms, int64_t* launches) {
+  if (!op || kernel < 0 || kernel >= K_NUM) return arg_error("invalid kernel timing query");
+  if (ms) *ms = op->kernel_ms[kernel];
+  if (launches) *launches = op->kernel_launches[kernel];
   return SGW_OK;
 }
 

@@ -75,11 +75,17 @@ struct BatchDev {
   long long ldx, ldr;
   int* ierr;
   int* iters;
+  const int* active;  // optional: 0 skips a right-hand side
+  zcd* zeta;          // optional: per-shift residual factors at exit
 };
 
 struct Workspace {
   DevBuf vec, coef, col, counter;
 };
+
+// Kernel kinds timed with CUDA events on the operator's stream.
+enum KernelKind { K_MSBICG_F64 = 0, K_MSBICG_F32 = 1, K_RESIDUAL_F64 = 2, K_NUM = 3 };
+constexpr int kMaxTimedLaunches = 64;
 
 }  // namespace sgw
 
@@ -92,6 +98,12 @@ struct sgw_operator {
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   double last_ms = 0.0;
   long long last_launches = 0;
+  // per-kernel timing of the last solve: event pairs recorded around launches
+  cudaEvent_t kev[2 * sgw::kMaxTimedLaunches] = {};
+  int kev_kind[sgw::kMaxTimedLaunches] = {};
+  int kev_used = 0;
+  double kernel_ms[sgw::K_NUM] = {};
+  long long kernel_launches[sgw::K_NUM] = {};
   double alpha_pv = 0.0;
   // tables
   sgw::DevBuf gcol, gi3, colpos, i1list, g2k64, g2k32, vrs64, vrs32, vkb64, vkb32, dvan64, dvan32, evq64, evq32,
@@ -129,6 +141,18 @@ inline long long col_elems(sgw_operator* op) {
   return op->kind == 1 ? (long long)pwview<T>(op).ncol * pwview<T>(op).ldz : 0;
 }
 
+
+// Event pair around one launch (no-op once the pool of pairs is used up).
+inline int ktime_begin(sgw_operator* op, int kind) {
+  if (op->kev_used >= kMaxTimedLaunches || !op->kev[0]) return -1;
+  const int i = op->kev_used++;
+  op->kev_kind[i] = kind;
+  cudaEventRecord(op->kev[2 * i], op->stream);
+  return i;
+}
+inline void ktime_end(sgw_operator* op, int i) {
+  if (i >= 0) cudaEventRecord(op->kev[2 * i + 1], op->stream);
+}
 
 template <typename T> sgw_status run_msbicg(sgw_operator* op, const BatchDev& b);
 template <typename T> sgw_status run_sgw(sgw_operator* op, const SgwArgs<T>& a);

@@ -79,10 +79,14 @@ sgw_status run_msbicg(sgw_operator* op, const BatchDev& b) {
   a.col_global = ws.col.as<cplx<T>>();
   a.col_slot = colsz;
   a.mode = mode;
+  a.active = b.active;
+  a.zeta = b.zeta;
   return with_applier<T>(op, [&](auto A, size_t smem) -> sgw_status {
     auto kern = msbicg_kernel<T, decltype(A)>;
     SGW_CK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const int t = ktime_begin(op, sizeof(T) == 8 ? K_MSBICG_F64 : K_MSBICG_F32);
     kern<<<nslots, kThreads, smem, op->stream>>>(a, A);
+    ktime_end(op, t);
     SGW_CK(cudaGetLastError());
     op->last_launches += 1;
     return SGW_OK;

@@ -1,9 +1,224 @@
-// Mixed-precision batched solve (complex64 Krylov, FP64 refinement).
+// Mixed-precision batched multishift solve (sgw_solve_batch, precision = 1).
+//
+// Rounds of restarted shifted BiCGStab(l) with collinear residuals:
+//   round 0:  r = b;  each later round: r = b - A(sigma_1) x_1 in FP64
+//   y^sigma  <- complex64 multishift solve of (A + sigma) y = r / |r| to a
+//               relative seed residual of 1e-5 (FP64 scalar and coefficient
+//               recurrences, FP32 vectors and operator applies)
+//   x^sigma  += |r| Z^sigma y^sigma   (FP64 accumulation)
+//   Z^sigma  *= zeta^sigma            (zeta = shifted/seed residual ratio of the round)
+// until the FP64 relative seed residual |b - A(sigma_1) x_1| / |b| is below the
+// refinement target (default 1e-9).  After each round the shifted residuals
+// are zeta-multiples of the seed residual up to FP32 rounding (Frommer's
+// shifted BiCGStab keeps residuals collinear), which is what lets one restart
+// serve every shift.  FP64 is used for the true seed residual, the shift
+// recurrences and the accumulation of x; everything else runs in FP32.
+#include <algorithm>
+#include <vector>
+
 #include "host.cuh"
+#include "launch.cuh"
 
 namespace sgw {
-sgw_status solve_mixed(sgw_operator*, const BatchDev&, int, double) {
-  set_error("mixed precision is not available yet");
-  return SGW_ERR_UNSUPPORTED;
+
+namespace {
+
+constexpr double kRoundRelThreshold = 1e-5;
+
+// |r|, r32 = r / |r| and the convergence flag, one CTA per right-hand side.
+__global__ void mx_normalise(int nrhs, int n, int npwx, const zcd* r, long long ldr, zcf* r32, double* scale,
+                             const double* bnorm, double target, int* active, int* nactive) {
+  __shared__ zcd red[32];
+  const int rhs = blockIdx.x;
+  if (rhs >= nrhs) return;
+  if (active[rhs] == 0) return;
+  const zcd* v = r + (size_t)rhs * ldr;
+  double p = 0.0;
+  for (int g = threadIdx.x; g < n; g += blockDim.x) p += abs2(v[g]);
+  const double nrm = sqrt(cta_sum(zcd{p, 0.0}, red).re);
+  const bool done = bnorm ? nrm <= target * bnorm[rhs] : false;
+  if (threadIdx.x == 0) {
+    scale[rhs] = nrm;
+    active[rhs] = done || nrm == 0.0 ? 0 : 1;
+    if (!done && nrm != 0.0) atomicAdd(nactive, 1);
+  }
+  const double inv = nrm > 0.0 ? 1.0 / nrm : 0.0;
+  zcf* o = r32 + (size_t)rhs * npwx;
+  for (int g = threadIdx.x; g < npwx; g += blockDim.x)
+    o[g] = g < n ? zcf{(float)(v[g].re * inv), (float)(v[g].im * inv)} : zcf{0.f, 0.f};
 }
+
+// x^sigma += scale Z^sigma y^sigma for active right-hand sides
+__global__ void mx_accumulate(int nrhs, int S, int n, int npwx, const zcf* y, zcd* x, long long ldx, long long ldr,
+                              const zcd* Z, const double* scale, const int* active, bool first) {
+  const long long total = (long long)nrhs * S * n;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total; e += (long long)gridDim.x * blockDim.x) {
+    const int g = (int)(e % n);
+    const long long rs = e / n;
+    const int s = (int)(rs % S), rhs = (int)(rs / S);
+    zcd* dst = x + (size_t)rhs * ldr + (size_t)s * ldx + g;
+    if (!active[rhs]) {  // a zero right-hand side never becomes active: its solution is zero
+      if (first) *dst = zcd{0.0, 0.0};
+      continue;
+    }
+    const zcf yv = y[((size_t)rhs * S + s) * npwx + g];
+    const zcd f = scale[rhs] * Z[(size_t)rhs * S + s];
+    const zcd add = f * zcd{(double)yv.re, (double)yv.im};
+    *dst = first ? add : *dst + add;
+  }
+}
+
+__global__ void mx_update_z(int nrhs, int S, zcd* Z, const zcd* zeta, const int* active, int* iters_total,
+                            const int* iters_round) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= nrhs * S) return;
+  const int rhs = e / S;
+  if (!active[rhs]) return;
+  Z[e] = Z[e] * zeta[e];
+  if (e % S == 0) iters_total[rhs] += iters_round[rhs];
+}
+
+__global__ void mx_init(int nrhs, int S, zcd* Z, int* active, int* iters_total) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e < nrhs * S) Z[e] = zcd{1.0, 0.0};
+  if (e < nrhs) {
+    active[e] = 1;
+    iters_total[e] = 0;
+  }
+}
+
+// r = b - A(sigma_1) x_1 in FP64 for active right-hand sides; one CTA each.
+template <class ApplyT>
+__global__ void __launch_bounds__(kThreads, 1)
+    mx_seed_residual(ApplyT A, int nrhs, int n, const zcd* bb, long long ldb, const zcd* sigma, long long lds,
+                     const zcd* x, long long ldr, zcd* r, long long ldrr, const int* active, zcd* col_global,
+                     long long col_slot) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  zcd* sm = reinterpret_cast<zcd*>(smem_raw);
+  zcd* col = A.col_in_smem ? sm + A.smem_small() : col_global + (size_t)blockIdx.x * col_slot;
+  A.setup(sm);
+  for (int rhs = blockIdx.x; rhs < nrhs; rhs += gridDim.x) {
+    if (!active[rhs]) continue;
+    zcd* out = r + (size_t)rhs * ldrr;
+    A.apply(x + (size_t)rhs * ldr, out, nullptr, sigma[(size_t)rhs * lds], sm, col);
+    const zcd* b = bb + (size_t)rhs * ldb;
+    for (int g = threadIdx.x; g < n; g += blockDim.x) out[g] = b[g] - out[g];
+    __syncthreads();
+  }
+}
+
+__global__ void mx_bnorm(int nrhs, int n, const zcd* bb, long long ldb, double* bnorm) {
+  __shared__ zcd red[32];
+  const int rhs = blockIdx.x;
+  if (rhs >= nrhs) return;
+  double p = 0.0;
+  for (int g = threadIdx.x; g < n; g += blockDim.x) p += abs2(bb[(size_t)rhs * ldb + g]);
+  const double s = sqrt(cta_sum(zcd{p, 0.0}, red).re);
+  if (threadIdx.x == 0) bnorm[rhs] = s;
+}
+
+__global__ void mx_finish(int nrhs, int S, int n, const zcd* x, long long ldx, long long ldr, const int* active,
+                          int* ierr, int max_rounds_hit) {
+  __shared__ int bad;
+  const int rhs = blockIdx.x;
+  if (rhs >= nrhs) return;
+  if (threadIdx.x == 0) bad = 0;
+  __syncthreads();
+  for (int e = threadIdx.x; e < S * n; e += blockDim.x) {
+    const zcd v = x[(size_t)rhs * ldr + (size_t)(e / n) * ldx + (e % n)];
+    if (v.re != v.re || v.im != v.im) bad = 1;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) ierr[rhs] = bad ? 2 : (active[rhs] && max_rounds_hit ? 1 : 0);
+}
+
+}  // namespace
+
+sgw_status solve_mixed(sgw_operator* op, const BatchDev& b, int refine_max, double refine_thr) {
+  const int R = b.nrhs, S = b.nshift, n = op->n, npwx = op->npwx;
+  if (refine_max <= 0) refine_max = 4;
+  if (refine_thr <= 0.0) refine_thr = 1e-9;
+  sgw_status s;
+  // workspace: r64 [R][npwx], r32 [R][npwx], y32 [R][S][npwx], Z/zeta [R][S], scale, bnorm, flags
+  DevBuf& m1 = op->st_misc;
+  DevBuf& m2 = op->st_misc2;
+  DevBuf& m3 = op->st_misc3;
+  const size_t r64_b = sizeof(zcd) * (size_t)R * npwx;
+  const size_t r32_b = sizeof(zcf) * (size_t)R * npwx;
+  const size_t y32_b = sizeof(zcf) * (size_t)R * S * npwx;
+  const size_t z_b = sizeof(zcd) * (size_t)R * S;
+  if ((s = m1.ensure(r64_b + r32_b)) != SGW_OK) return s;
+  if ((s = m2.ensure(y32_b)) != SGW_OK) return s;
+  if ((s = m3.ensure(2 * z_b + 2 * sizeof(double) * R + 3 * sizeof(int) * R + 256)) != SGW_OK) return s;
+  zcd* r64 = m1.as<zcd>();
+  zcf* r32 = reinterpret_cast<zcf*>(reinterpret_cast<unsigned char*>(m1.p) + r64_b);
+  zcf* y32 = m2.as<zcf>();
+  unsigned char* p3 = reinterpret_cast<unsigned char*>(m3.p);
+  zcd* Z = reinterpret_cast<zcd*>(p3);
+  zcd* zeta = Z + (size_t)R * S;
+  double* scale = reinterpret_cast<double*>(zeta + (size_t)R * S);
+  double* bnorm = scale + R;
+  int* active = reinterpret_cast<int*>(bnorm + R);
+  int* iters_round = active + R;
+  int* nactive = iters_round + R;
+  int* iters_total = b.iters;
+  const zcd* bb = reinterpret_cast<const zcd*>(b.bb);
+  zcd* x = reinterpret_cast<zcd*>(b.xx);
+  const int tb = 256;
+  mx_init<<<(R * S + tb - 1) / tb, tb, 0, op->stream>>>(R, S, Z, active, iters_total);
+  mx_bnorm<<<R, tb, 0, op->stream>>>(R, n, bb, b.ldb, bnorm);
+  op->last_launches += 2;
+  // round 0 right-hand side: b itself
+  SGW_CK(cudaMemcpy2DAsync(r64, sizeof(zcd) * npwx, bb, sizeof(zcd) * b.ldb, sizeof(zcd) * n, R,
+                           cudaMemcpyDeviceToDevice, op->stream));
+  int rounds_done = 0;
+  bool all_done = false;
+  for (int round = 0; round <= refine_max; ++round) {
+    SGW_CK(cudaMemsetAsync(nactive, 0, sizeof(int), op->stream));
+    mx_normalise<<<R, tb, 0, op->stream>>>(R, n, npwx, r64, npwx, r32, scale, round == 0 ? nullptr : bnorm,
+                                           refine_thr, active, nactive);
+    op->last_launches += 1;
+    int h_active = 0;
+    SGW_CK(cudaMemcpyAsync(&h_active, nactive, sizeof(int), cudaMemcpyDeviceToHost, op->stream));
+    SGW_CK(cudaStreamSynchronize(op->stream));
+    if (h_active == 0) {
+      all_done = true;
+      break;
+    }
+    if (round == refine_max) break;
+    BatchDev bf{R, S, b.lmax, b.max_iter, b.history_iters, kRoundRelThreshold, r32, npwx, b.sigma, b.lds, y32,
+                npwx, (long long)S * npwx, b.ierr, iters_round, active, zeta};
+    if ((s = run_msbicg<float>(op, bf)) != SGW_OK) return s;
+    mx_accumulate<<<std::min(4096, (int)(((long long)R * S * n + tb - 1) / tb)), tb, 0, op->stream>>>(
+        R, S, n, npwx, y32, x, b.ldx, b.ldr, Z, scale, active, round == 0);
+    mx_update_z<<<(R * S + tb - 1) / tb, tb, 0, op->stream>>>(R, S, Z, zeta, active, iters_total, iters_round);
+    op->last_launches += 2;
+    // FP64 true residual of the seed system
+    s = with_applier<double>(op, [&](auto A, size_t smem) -> sgw_status {
+      auto kern = mx_seed_residual<decltype(A)>;
+      const long long colsz = (op->kind == 1 && !op->shape64.col_in_smem) ? col_elems<double>(op) : 0;
+      const int grid = std::min(R, op->num_sms);
+      if (colsz) {
+        sgw_status s2 = op->ws64.col.ensure(sizeof(zcd) * colsz * grid);
+        if (s2 != SGW_OK) return s2;
+      }
+      SGW_CK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      const int t = ktime_begin(op, K_RESIDUAL_F64);
+      kern<<<grid, kThreads, smem, op->stream>>>(A, R, n, bb, b.ldb, b.sigma, b.lds, x, b.ldr, r64, npwx, active,
+                                                 op->ws64.col.as<zcd>(), colsz);
+      ktime_end(op, t);
+      SGW_CK(cudaGetLastError());
+      op->last_launches += 1;
+      return SGW_OK;
+    });
+    if (s != SGW_OK) return s;
+    rounds_done = round + 1;
+  }
+  (void)rounds_done;
+  mx_finish<<<R, tb, 0, op->stream>>>(R, S, n, x, b.ldx, b.ldr, active, b.ierr, all_done ? 0 : 1);
+  op->last_launches += 1;
+  SGW_CK(cudaGetLastError());
+  return SGW_OK;
+}
+
 }  // namespace sgw

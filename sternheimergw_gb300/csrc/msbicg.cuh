@@ -57,6 +57,8 @@ struct SolverArgs {
   cplx<T>* col_global; // [slot][ncol*ldz] when the column store does not fit in shared memory
   long long col_slot;
   int mode;            // 0 coefficient-space shifts, 1 explicit shift vectors
+  const int* active;   // optional [rhs]: 0 skips the right-hand side
+  zcd* zeta;           // optional [rhs][nshift]: residual factor 1/(theta phi) of each shift at exit
 };
 
 // Shared seed scalars of the MR part (tau, nu, gammas), 1-based like the reference.
@@ -595,6 +597,11 @@ __device__ void solve_one(const SolverArgs<T>& a, const ApplyT& A, int rhs, int 
       const int s = (int)(e / n), g = (int)(e - (long long)s * n);
       xout[(size_t)(s + 1) * a.ldx + g] = XSV(s)[g];
     }
+  if (a.zeta) {  // shifted residual = zeta * seed residual (collinear residuals of the shifted method)
+    zcd* z = a.zeta + (size_t)rhs * S;
+    if (tid == 0) z[0] = zcd{1.0, 0.0};
+    for (int s = tid; s < Sm1; s += nt) z[s + 1] = SCAL(s, SC_THETA) * SCAL(s, SC_PHI);
+  }
   __syncthreads();
   if (tid == 0) ss.flag = 0;
   __syncthreads();
@@ -632,6 +639,7 @@ __global__ void __launch_bounds__(kThreads, 1) msbicg_kernel(SolverArgs<T> a, Ap
     const int rhs = s_rhs;
     __syncthreads();
     if (rhs >= a.nrhs) break;
+    if (a.active && !a.active[rhs]) continue;
     solve_one<T, ApplyT>(a, A, rhs, blockIdx.x, sm, col, ss);
   }
 }

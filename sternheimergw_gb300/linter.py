@@ -91,3 +91,48 @@ def green_shifts(mu, coul_freq):
     coul = np.asarray(coul_freq, dtype=np.complex128)
     omega = np.concatenate([mu + coul, mu - coul])
     return -omega
+
+
+def chi_matrix(bb, x, freq, weight=1.0):
+    """Density response chi[G', G](omega) = -sum_v <b_v^{G'} | x_v^G(omega)>, +-omega averaged.
+
+    The projection of what solve_linter accumulates into drhoscf for each perturbation
+    (incdrhoscf after the +-omega average, solve_linter.f90:462-497) projected on
+    the perturbation set: with b = -P_c Delta V psi_v and Delta psi in the
+    conduction space, <Delta V_{G'} psi_v | Delta psi_v^G> = -<b^{G'} | x^G>.
+    bb: (npert, nocc, n); x: (npert, nocc, S, n).  Works on numpy or torch.
+    Returns (nfreq, npert, npert).
+    """
+    if type(bb).__module__.startswith("torch"):
+        import torch
+        c = -torch.einsum("pvn,qvsn->spq", bb.conj(), x) * weight
+        nf = len(freq)
+        out = c[:nf].clone()
+        if abs(complex(freq[0])) < 1e-14:
+            out[1:] = 0.5 * out[1:] + 0.5 * c[nf:]
+        else:
+            out = 0.5 * out + 0.5 * c[nf:]
+        return out
+    c = -np.einsum("pvn,qvsn->spq", np.conj(bb), x) * weight
+    return np.moveaxis(average_pm(np.moveaxis(c, 0, -1), freq), -1, 0)
+
+
+def coulomb_v(system):
+    """Bare Coulomb 8 pi / (Omega |q+G|^2) (Ry) for each perturbation G."""
+    import math
+    bmat = {"fcc": np.array([[-1, -1, 1], [1, 1, 1], [-1, 1, -1]]), "sc8": np.eye(3), "sc2": np.eye(3)}[system["lattice"]]
+    qg = (system["gpert"] @ bmat + system["qvec"][None, :]) * (2 * math.pi / system["alat"])
+    return 8 * math.pi / (system["omega"] * np.sum(qg ** 2, 1))
+
+
+def w_from_chi(chi, v):
+    """W(omega) = (1 - v chi)^-1 v on the perturbation set (invert_epsilon.f90:23-90, coulpade.f90)."""
+    if type(chi).__module__.startswith("torch"):
+        import torch
+        vv = torch.as_tensor(v, dtype=chi.dtype, device=chi.device)
+        eye = torch.eye(chi.shape[-1], dtype=chi.dtype, device=chi.device)
+        eps = eye[None] - vv[None, :, None] * chi
+        return torch.linalg.solve(eps, torch.diag(vv)[None].expand_as(eps))
+    eye = np.eye(chi.shape[-1])
+    eps = eye[None] - v[None, :, None] * chi
+    return np.linalg.solve(eps, np.broadcast_to(np.diag(v), eps.shape))

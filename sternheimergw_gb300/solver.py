@@ -98,6 +98,13 @@ class _Operator:
                                                    xm.shape[1], _p(xm), self.n, _p(out), self.n), "sgw_operator_apply")
         return out[:, 0] if one else out
 
+    def kernel_timing(self, kernel):
+        """(ms, launches) of one kernel in the last solve_batch: 0 FP64 solve, 1 FP32 solve, 2 FP64 seed residual."""
+        ms = C.c_double(0)
+        n = C.c_int64(0)
+        _capi.check(_capi.lib().sgw_kernel_timing(self.handle, int(kernel), C.byref(ms), C.byref(n)), "sgw_kernel_timing")
+        return ms.value, n.value
+
     def last_timing(self):
         ms = C.c_double(0)
         n = C.c_int64(0)

@@ -187,3 +187,41 @@ def test_device_pointer_batch(c0):
     xd, ierrd, itd = sg.solve_batch(op, torch.from_numpy(bb).cuda(), torch.from_numpy(sh).cuda(), threshold=1e-10)
     assert (ierrd.cpu().numpy() == ierrh).all()
     assert rel(xd.cpu().numpy(), xh) < 1e-14
+
+
+def test_mixed_c0(c0):
+    """Mixed precision: FP64 seed residual <= 1e-9 and the response within 1e-6 of FP64."""
+    s, f, op, ops = c0
+    bb = linter.coulomb_rhs(s, 0)
+    sh = linter.coulomb_shifts(s, f)
+    x64, ierr64, _ = sg.solve_batch(op, bb, sh, threshold=1e-10)
+    xm, ierr, iters = sg.solve_batch(op, bb, sh, threshold=1e-10, precision=1)
+    assert (ierr == 0).all() and (iters > 0).all()
+    for r in range(bb.shape[0]):
+        res = op.apply(sh[r, 0], xm[r, 0]) - bb[r]
+        assert np.linalg.norm(res) / np.linalg.norm(bb[r]) <= 1e-9
+    c64 = linter.chi_matrix(bb[None], x64[None], f)
+    cm = linter.chi_matrix(bb[None], xm[None], f)
+    assert np.linalg.norm(cm - c64) / np.linalg.norm(c64) < 1e-6
+
+
+def test_mixed_w_error_c4(gpu_lib):
+    """W(G, G'; omega) from the mixed solve within 1e-6 (normwise) of FP64 on the c4 system."""
+    from sternheimergw_gb300 import synth
+    s, f = synth.config("c4")
+    op = sg.PlaneWaveOperator(s)
+    npert, nocc = len(s["gpert"]), s["nocc"]
+    B = np.stack([linter.coulomb_rhs(s, ip) for ip in range(npert)])
+    sh1 = linter.coulomb_shifts(s, f)
+    bb = B.reshape(npert * nocc, -1)
+    sh = np.tile(sh1, (npert, 1))
+    x64, e64, _ = sg.solve_batch(op, bb, sh, threshold=1e-10)
+    xm, em, _ = sg.solve_batch(op, bb, sh, threshold=1e-10, precision=1)
+    assert (e64 == 0).all() and (em == 0).all()
+    X64 = x64.reshape(npert, nocc, sh.shape[1], -1)
+    XM = xm.reshape(npert, nocc, sh.shape[1], -1)
+    v = linter.coulomb_v(s)
+    W64 = linter.w_from_chi(linter.chi_matrix(B, X64, f), v)
+    WM = linter.w_from_chi(linter.chi_matrix(B, XM, f), v)
+    err = np.linalg.norm(WM - W64, axis=(1, 2)) / np.linalg.norm(W64, axis=(1, 2))
+    assert err.max() < 1e-6, err.max()
