@@ -284,6 +284,8 @@ def run_gpu(args, rank, world):
     torch.cuda.set_device(dev)
     _capi.lib(build_if_missing=False)
     s, f, bb, sigma = make_workload()
+    if args.nrhs:
+        bb, sigma = bb[:args.nrhs], sigma[:args.nrhs]
     nrhs, S = sigma.shape
     n = s["npw"]
     op = sg.PlaneWaveOperator(s)
@@ -301,10 +303,20 @@ def run_gpu(args, rank, world):
     barrier()
     with ClockSampler(dev) as clk:
         t0 = time.time()
-        p64 = time_path(op, bb_d, sg_d, x64_d, 0, args.warmup, args.steps, l2, "fp64")
-        pm = time_path(op, bb_d, sg_d, xm_d, 1, args.warmup, args.steps, l2, "mixed")
+        p64 = pm = None
+        if args.precision in ("both", "fp64"):
+            p64 = time_path(op, bb_d, sg_d, x64_d, 0, args.warmup, args.steps, l2, "fp64")
+        if args.precision in ("both", "mixed"):
+            pm = time_path(op, bb_d, sg_d, xm_d, 1, args.warmup, args.steps, l2, "mixed")
         barrier()
         wall = time.time() - t0
+    if args.no_extras or p64 is None or pm is None:
+        if rank == 0:
+            out = {"profiling_run": True, "nrhs": nrhs,
+                   "fp64_ms": p64["ms"] if p64 else None, "mixed_ms": pm["ms"] if pm else None,
+                   "clocks": clk.summary()}
+            print(json.dumps(out), flush=True)
+        return out
     ms_m, ms_64 = pm["ms"], p64["ms"]
     if world > 1:
         t = torch.tensor([ms_m, ms_64], device="cuda")
@@ -387,6 +399,11 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--nrhs", type=int, default=0,
+                    help="solve only the first N right-hand sides (reduced case for profiling; 0 = all)")
+    ap.add_argument("--precision", default="both", choices=["both", "fp64", "mixed"])
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the e2e leg, the W-error check, the peak probes and the CPU baseline (profiling runs)")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))
