@@ -311,6 +311,7 @@ def run_gpu(args, rank, world):
         barrier()
         wall = time.time() - t0
     if args.no_extras or p64 is None or pm is None:
+        out = None
         if rank == 0:
             out = {"profiling_run": True, "nrhs": nrhs,
                    "fp64_ms": p64["ms"] if p64 else None, "mixed_ms": pm["ms"] if pm else None,
