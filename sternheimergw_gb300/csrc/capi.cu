@@ -7,6 +7,7 @@
 #include <vector>
 
 #include "host.cuh"
+#include "fftreg.cuh"
 #include "sgwsolver.cuh"
 
 namespace sgw {
@@ -60,23 +61,38 @@ template <typename T>
 static PwShape choose_shape(const PwView<T>& v, size_t smem_optin) {
   const size_t static_bytes = sizeof(SeedShared) + 64;
   const size_t budget = smem_optin > static_bytes ? smem_optin - static_bytes : 0;
+  const size_t colb = (size_t)v.ncol * v.ldz * sizeof(cplx<T>);
+  auto small = [&](int ng) { return (size_t)pw_smem_small(v, ng) * sizeof(cplx<T>); };
   PwShape s;
+  if (fft_reg_supported<T>(v.nr1) && fft_reg_supported<T>(v.nr2) && fft_reg_supported<T>(v.nr3)) {
+    // line FFT: as many planes in flight as shared memory holds (column store first)
+    s.lines = true;
+    for (bool in_smem : {true, false}) {
+      int best = 0;
+      for (int pf = 1; pf <= v.nr3; ++pf)
+        if (small(pf) + (in_smem ? colb : 0) <= budget) best = pf;
+      if (best >= (in_smem ? 2 : 1)) {
+        s.ng = best;
+        s.col_in_smem = in_smem;
+        s.smem = small(best) + (in_smem ? colb : 0);
+        return s;
+      }
+    }
+    s.lines = false;
+  }
   for (int ng : {4, 2, 1}) {
-    const size_t small = (size_t)pw_smem_small(v, ng) * sizeof(cplx<T>);
-    const size_t colb = (size_t)v.ncol * v.ldz * sizeof(cplx<T>);
-    if (small + colb <= budget) {
+    if (small(ng) + colb <= budget) {
       s.ng = ng;
       s.col_in_smem = true;
-      s.smem = small + colb;
+      s.smem = small(ng) + colb;
       return s;
     }
   }
   for (int ng : {4, 2, 1}) {
-    const size_t small = (size_t)pw_smem_small(v, ng) * sizeof(cplx<T>);
-    if (small <= budget) {
+    if (small(ng) <= budget) {
       s.ng = ng;
       s.col_in_smem = false;
-      s.smem = small;
+      s.smem = small(ng);
       return s;
     }
   }

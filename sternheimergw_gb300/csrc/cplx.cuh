@@ -44,3 +44,22 @@ template <typename T> SGW_HD cplx<T> operator/(cplx<T> a, cplx<T> b) {
 template <typename T> SGW_HD T abs2(cplx<T> a) { return a.re * a.re + a.im * a.im; }
 
 template <typename To, typename From> SGW_HD cplx<To> ccast(cplx<From> a) { return {(To)a.re, (To)a.im}; }
+
+#if defined(__CUDACC__)
+__device__ __forceinline__ double fmad_(double a, double b, double c) { return __fma_rn(a, b, c); }
+__device__ __forceinline__ float fmad_(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+// acc += a * b with four fused multiply-adds
+template <typename T> __device__ __forceinline__ void cfma(cplx<T>& acc, cplx<T> a, cplx<T> b) {
+  acc.re = fmad_(a.re, b.re, acc.re);
+  acc.re = fmad_(-a.im, b.im, acc.re);
+  acc.im = fmad_(a.re, b.im, acc.im);
+  acc.im = fmad_(a.im, b.re, acc.im);
+}
+// acc += conj(a) * b
+template <typename T> __device__ __forceinline__ void cfma_conj(cplx<T>& acc, cplx<T> a, cplx<T> b) {
+  acc.re = fmad_(a.re, b.re, acc.re);
+  acc.re = fmad_(a.im, b.im, acc.re);
+  acc.im = fmad_(a.re, b.im, acc.im);
+  acc.im = fmad_(-a.im, b.re, acc.im);
+}
+#endif

@@ -58,7 +58,8 @@ struct DevBuf {
 
 // Pruned-FFT launch shape of a plane-wave operator in one precision.
 struct PwShape {
-  int ng = 1;            // plane groups
+  int ng = 1;            // plane groups (stage FFT) or planes in flight (line FFT)
+  bool lines = false;    // line-per-thread register FFT
   bool col_in_smem = true;
   size_t smem = 0;       // dynamic shared memory bytes
 };
@@ -120,8 +121,8 @@ struct sgw_operator {
 
 namespace sgw {
 template <typename T> struct Ipt;
-template <> struct Ipt<double> { static constexpr int v = 2; };
-template <> struct Ipt<float> { static constexpr int v = 4; };
+template <> struct Ipt<double> { static constexpr int v = 1; };
+template <> struct Ipt<float> { static constexpr int v = 1; };
 
 template <typename T> PwView<T>& pwview(sgw_operator* op);
 template <> inline PwView<double>& pwview<double>(sgw_operator* op) { return op->pw64; }

@@ -22,7 +22,8 @@ static sgw_status with_applier(sgw_operator* op, F&& f) {
     set_error("FFT box too large for shared memory");
     return SGW_ERR_UNSUPPORTED;
   }
-  return f(PwApply<T, I>{v, sh.col_in_smem, sh.ng}, sh.smem);
+  if (sh.lines) return f(PwApply<T, I, true>{v, sh.col_in_smem, sh.ng}, sh.smem);
+  return f(PwApply<T, I, false>{v, sh.col_in_smem, sh.ng}, sh.smem);
 }
 
 template <typename T>
@@ -82,10 +83,11 @@ sgw_status run_msbicg(sgw_operator* op, const BatchDev& b) {
   a.active = b.active;
   a.zeta = b.zeta;
   return with_applier<T>(op, [&](auto A, size_t smem) -> sgw_status {
-    auto kern = msbicg_kernel<T, decltype(A)>;
+    constexpr int NT = CtaThreads<T>::v;
+    auto kern = msbicg_kernel<T, decltype(A), NT>;
     SGW_CK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     const int t = ktime_begin(op, sizeof(T) == 8 ? K_MSBICG_F64 : K_MSBICG_F32);
-    kern<<<nslots, kThreads, smem, op->stream>>>(a, A);
+    kern<<<nslots, NT, smem, op->stream>>>(a, A);
     ktime_end(op, t);
     SGW_CK(cudaGetLastError());
     op->last_launches += 1;
@@ -98,9 +100,10 @@ sgw_status run_msbicg(sgw_operator* op, const BatchDev& b) {
 template <typename T>
 sgw_status run_sgw(sgw_operator* op, const SgwArgs<T>& a) {
   return with_applier<T>(op, [&](auto A, size_t smem) -> sgw_status {
-    auto kern = sgw_solver_kernel<T, decltype(A)>;
+    constexpr int NT = CtaThreads<T>::v;
+    auto kern = sgw_solver_kernel<T, decltype(A), NT>;
     SGW_CK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    kern<<<1, kThreads, smem, op->stream>>>(a, A);
+    kern<<<1, NT, smem, op->stream>>>(a, A);
     SGW_CK(cudaGetLastError());
     op->last_launches += 1;
     return SGW_OK;
@@ -117,9 +120,10 @@ sgw_status run_apply(sgw_operator* op, int m, const cplx<T>* x, long long ldi, c
     if (s != SGW_OK) return s;
   }
   return with_applier<T>(op, [&](auto A, size_t smem) -> sgw_status {
-    auto kern = apply_kernel<T, decltype(A)>;
+    constexpr int NT = CtaThreads<T>::v;
+    auto kern = apply_kernel<T, decltype(A), NT>;
     SGW_CK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    kern<<<grid, kThreads, smem, op->stream>>>(A, m, x, ldi, ax, ldo, sigma, ws.col.as<cplx<T>>(), colsz);
+    kern<<<grid, NT, smem, op->stream>>>(A, m, x, ldi, ax, ldo, sigma, ws.col.as<cplx<T>>(), colsz);
     SGW_CK(cudaGetLastError());
     op->last_launches += 1;
     return SGW_OK;
@@ -194,9 +198,10 @@ sgw_status run_msbicg_in(sgw_operator* op, const BatchDev& b, unsigned char* reg
     // the region keeps the previous call's contents: the work counter must start at zero
     SGW_CK(cudaMemsetAsync(region, 0, sizeof(int), op->stream));
     return with_applier<T>(op, [&](auto A, size_t smem) -> sgw_status {
-      auto kern = msbicg_kernel<T, decltype(A)>;
+      constexpr int NT = CtaThreads<T>::v;
+    auto kern = msbicg_kernel<T, decltype(A), NT>;
       SGW_CK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-      kern<<<nslots, kThreads, smem, op->stream>>>(a, A);
+      kern<<<nslots, NT, smem, op->stream>>>(a, A);
       SGW_CK(cudaGetLastError());
       op->last_launches += 1;
       return SGW_OK;

@@ -89,7 +89,7 @@ __global__ void mx_init(int nrhs, int S, zcd* Z, int* active, int* iters_total) 
 
 // r = b - A(sigma_1) x_1 in FP64 for active right-hand sides; one CTA each.
 template <class ApplyT>
-__global__ void __launch_bounds__(kThreads, 1)
+__global__ void __launch_bounds__(CtaThreads<double>::v, 1)
     mx_seed_residual(ApplyT A, int nrhs, int n, const zcd* bb, long long ldb, const zcd* sigma, long long lds,
                      const zcd* x, long long ldr, zcd* r, long long ldrr, const int* active, zcd* col_global,
                      long long col_slot) {
@@ -204,7 +204,7 @@ sgw_status solve_mixed(sgw_operator* op, const BatchDev& b, int refine_max, doub
       }
       SGW_CK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
       const int t = ktime_begin(op, K_RESIDUAL_F64);
-      kern<<<grid, kThreads, smem, op->stream>>>(A, R, n, bb, b.ldb, b.sigma, b.lds, x, b.ldr, r64, npwx, active,
+      kern<<<grid, CtaThreads<double>::v, smem, op->stream>>>(A, R, n, bb, b.ldb, b.sigma, b.lds, x, b.ldr, r64, npwx, active,
                                                  op->ws64.col.as<zcd>(), colsz);
       ktime_end(op, t);
       SGW_CK(cudaGetLastError());

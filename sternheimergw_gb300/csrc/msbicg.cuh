@@ -31,6 +31,9 @@
 namespace sgw {
 
 constexpr int kMaxL = 16;
+// CTA size: 256 threads, so a thread may hold up to 255 registers (a whole
+// FFT line in the register path).
+template <typename T> struct CtaThreads { static constexpr int v = 256; };
 constexpr int kThreads = 512;
 
 template <typename T>
@@ -78,7 +81,7 @@ struct SeedShared {
 // Layout of the FP64 coefficient slot (all per-shift arrays are [field][P]).
 struct CoefLayout {
   int l, D, Db, P, Kcap;
-  long long o_scal, o_mu, o_us, o_xinc, o_xa, o_ub, o_gs, o_gp, o_gpp, o_cr, o_cu, total;
+  long long o_scal, o_mu, o_us, o_xinc, o_xa, o_ub, o_gs, o_gp, o_gpp, o_cr, o_cu, o_cvt, total;
   __host__ __device__ CoefLayout(int l_, int P_, int Kcap_) : l(l_), P(P_), Kcap(Kcap_) {
     D = 2 * l + 3;
     Db = 2 * l + 2;
@@ -94,6 +97,7 @@ struct CoefLayout {
     o_gpp = o; o += (long long)(l + 1) * P;
     o_cr = o; o += (long long)(l + 1) * Db;          // seed coefficient vectors (shared by the CTA)
     o_cu = o; o += (long long)(l + 1) * Db;
+    o_cvt = o; o += (long long)Kcap * P;             // working-precision copy of XA/UB for the basis product
     total = o;
   }
 };
@@ -102,18 +106,26 @@ enum { SC_PHIOLD = 0, SC_PHI, SC_THETA, SC_SIG, SC_ALPHA, SC_UC, SC_XD, SC_BETA,
 
 // --- operator adaptors -------------------------------------------------------
 
-template <typename T, int IPT>
+template <typename T, int IPT, bool LINES>
 struct PwApply {
   PwView<T> op;
   bool col_in_smem;
-  int ng;  // plane groups
+  int ng;  // plane groups (stage FFT) or planes in flight (line FFT, LINES)
   __device__ int smem_small() const { return pw_smem_small(op, ng); }
+  // shared memory the basis product may use once the applies are done (the plane buffers)
+  __device__ cplx<T>* scratch(cplx<T>* sm, int& elems) const {
+    elems = ng * op.nr2 * op.pitch;
+    return sm + op.nr1 + op.nr2 + op.nr3 + op.nkb + op.nocc;
+  }
   __device__ void setup(cplx<T>* sm) const {
     for (int e = threadIdx.x; e < op.nr1 + op.nr2 + op.nr3; e += blockDim.x) sm[e] = op.tw[e];
     __syncthreads();
   }
   __device__ void apply(const cplx<T>* in, cplx<T>* out, cplx<T>* out2, zcd sigma, cplx<T>* sm, cplx<T>* col) const {
-    pw_apply_cta<T, IPT>(op, ng, in, out, out2, sigma, sm, col);
+    if constexpr (LINES)
+      pw_apply_cta_lines<T>(op, ng, in, out, out2, sigma, sm, col);
+    else
+      pw_apply_cta<T, IPT>(op, ng, in, out, out2, sigma, sm, col);
   }
 };
 
@@ -122,6 +134,10 @@ struct DenseApply {
   DenseView<T> op;
   bool col_in_smem;
   __device__ int smem_small() const { return op.n; }
+  __device__ cplx<T>* scratch(cplx<T>* sm, int& elems) const {
+    elems = op.n;
+    return sm;
+  }
   __device__ void setup(cplx<T>*) const {}
   __device__ void apply(const cplx<T>* in, cplx<T>* out, cplx<T>* out2, zcd sigma, cplx<T>* sm, cplx<T>*) const {
     dense_apply_cta<T>(op, in, out, out2, sigma, sm);
@@ -137,7 +153,7 @@ __device__ __forceinline__ void v_copy(cplx<T>* y, const cplx<T>* x, int n) {
 template <typename T>
 __device__ __forceinline__ void v_axpy(cplx<T>* y, zcd a, const cplx<T>* x, int n) {
   const cplx<T> aa = ccast<T>(a);
-  for (int g = threadIdx.x; g < n; g += blockDim.x) y[g] += aa * x[g];
+  for (int g = threadIdx.x; g < n; g += blockDim.x) cfma(y[g], aa, x[g]);
 }
 
 // --- the coefficient-space replay of one shifted system ---------------------
@@ -203,102 +219,144 @@ __device__ inline void shift_mr_scalars(const ShiftRef& sh, const CoefLayout& L,
   sh.at(L.o_scal, SC_F1) = zcd{1.0, 0.0} / psi;
 }
 
-// Mode 0: the shift's vector updates on coefficient vectors (cr = seed r_i).
+// Mode 0: the shifts' updates on coefficient vectors (cr = seed r_i).  After
+// the scalar phase (one thread per shift) every coefficient index q of every
+// shift is independent, so these run one thread per (q, shift) pair with short,
+// coalesced accesses ([field][P] layout, shift fastest).
+
 // bicgstab.f90:641-662 at step j, before the seed's r update.
-__device__ inline void replay_bicg1(const ShiftRef& sh, const CoefLayout& L, const zcd* cr, int j) {
+__device__ __forceinline__ void replay_bicg1_q(const ShiftRef& sh, const CoefLayout& L, const zcd* cr, int j, int q) {
   const zcd beta_s = sh.at(L.o_scal, SC_BETA), alpha_s = sh.at(L.o_scal, SC_ALPHA), factor = sh.at(L.o_scal, SC_F1);
   const int D = L.D, Db = L.Db;
+  const bool b = q < Db;
   for (int i = 0; i <= j; ++i) {  // L15: u_i = -beta u_i + factor r_i
-    for (int q = 0; q < Db; ++q) {
-      zcd& u = sh.at(L.o_us, i * D + q);
-      u = -beta_s * u;
-      u += factor * cr[i * Db + q];
-    }
-    zcd& uc = sh.at(L.o_us, i * D + Db);
-    uc = -beta_s * uc;
+    zcd& u = sh.at(L.o_us, i * D + q);
+    zcd v = -beta_s * u;
+    if (b) v += factor * cr[i * Db + q];
+    u = v;
   }
-  for (int q = 0; q < D; ++q) sh.at(L.o_xinc, q) += alpha_s * sh.at(L.o_us, q);  // L17
-  for (int q = 0; q < Db; ++q) sh.at(L.o_us, (j + 1) * D + q) = factor * cr[j * Db + q];  // L19
-  sh.at(L.o_us, (j + 1) * D + Db) = zcd{0.0, 0.0};
+  sh.at(L.o_xinc, q) += alpha_s * sh.at(L.o_us, q);                                    // L17
+  sh.at(L.o_us, (j + 1) * D + q) = b ? factor * cr[j * Db + q] : zcd{0.0, 0.0};         // L19
 }
 
 // bicgstab.f90:692-696 after the seed's r update of step j.
-__device__ inline void replay_bicg2(const ShiftRef& sh, const CoefLayout& L, const zcd* cr, int j) {
+__device__ __forceinline__ void replay_bicg2_q(const ShiftRef& sh, const CoefLayout& L, const zcd* cr, int j, int q) {
   const zcd factor = sh.at(L.o_scal, SC_F2);
   const zcd inv_alpha = zcd{1.0, 0.0} / sh.at(L.o_scal, SC_ALPHA);
   const zcd msig = -sh.at(L.o_scal, SC_SIG);
   const int D = L.D, Db = L.Db;
-  for (int q = 0; q < D; ++q) {
-    zcd u = sh.at(L.o_us, (j + 1) * D + q);
-    if (q < Db) u += factor * cr[j * Db + q];
-    u = inv_alpha * u;
-    u += msig * sh.at(L.o_us, j * D + q);
-    sh.at(L.o_us, (j + 1) * D + q) = u;
-  }
+  zcd u = sh.at(L.o_us, (j + 1) * D + q);
+  if (q < Db) u += factor * cr[j * Db + q];
+  u = inv_alpha * u;
+  u += msig * sh.at(L.o_us, j * D + q);
+  sh.at(L.o_us, (j + 1) * D + q) = u;
 }
 
 // bicgstab.f90:886-911 on coefficient vectors; cr holds the seed r_j after Gram-Schmidt.
-__device__ inline void replay_mr(const ShiftRef& sh, const CoefLayout& L, const zcd* cr, const SeedShared& ss) {
+__device__ __forceinline__ void replay_mr_q(const ShiftRef& sh, const CoefLayout& L, const zcd* cr, const SeedShared& ss,
+                                            int q) {
   const int l = L.l, D = L.D, Db = L.Db;
-  const zcd f0 = sh.at(L.o_gpp, 0);
-  for (int q = 0; q < Db; ++q) sh.at(L.o_xinc, q) += f0 * cr[q];
-  for (int q = 0; q < D; ++q) sh.at(L.o_us, q) += (-ss.gamma[l]) * sh.at(L.o_us, l * D + q);
+  const bool b = q < Db;
+  zcd x = sh.at(L.o_xinc, q);
+  zcd u0 = sh.at(L.o_us, q);
+  if (b) x += sh.at(L.o_gpp, 0) * cr[q];
+  u0 += (-ss.gamma[l]) * sh.at(L.o_us, l * D + q);
   for (int jj = 1; jj <= l - 1; ++jj) {
-    for (int q = 0; q < D; ++q) sh.at(L.o_us, q) += (-ss.gamma[jj]) * sh.at(L.o_us, jj * D + q);
-    const zcd f = sh.at(L.o_gpp, jj);
-    for (int q = 0; q < Db; ++q) sh.at(L.o_xinc, q) += f * cr[jj * Db + q];
+    u0 += (-ss.gamma[jj]) * sh.at(L.o_us, jj * D + q);
+    if (b) x += sh.at(L.o_gpp, jj) * cr[jj * Db + q];
   }
-  const zcd ipsi = sh.at(L.o_scal, SC_F1);  // L34
-  for (int q = 0; q < D; ++q) sh.at(L.o_us, q) = ipsi * sh.at(L.o_us, q);
+  sh.at(L.o_xinc, q) = x;
+  sh.at(L.o_us, q) = sh.at(L.o_scal, SC_F1) * u0;  // L34: u_0 / psi
 }
 
 // Fold the finished outer iteration (basis block at kw) into the window
-// accumulators: x_inc over the window (XA, Xd) and u_0^sigma (UB, Uc).
-__device__ inline void replay_window(const ShiftRef& sh, const CoefLayout& L, int kw) {
-  const int D = L.D, Db = L.Db;
-  const zcd d = sh.at(L.o_xinc, Db);
-  const zcd c = sh.at(L.o_us, Db);
-  zcd& Uc = sh.at(L.o_scal, SC_UC);
-  zcd& Xd = sh.at(L.o_scal, SC_XD);
-  for (int k = 0; k < kw; ++k) {
-    zcd& ub = sh.at(L.o_ub, k);
-    sh.at(L.o_xa, k) += d * ub;
-    ub = c * ub;
+// accumulators: x_inc over the window (XA, Xd) and u_0^sigma (UB, Uc).  Entry
+// e of the CTA-wide loop is (k, shift) for the old window part, then (q, shift)
+// for the new block; the carries Xd, Uc are updated by the shift's own thread
+// once every thread has read them.
+__device__ __forceinline__ void replay_window_cta(zcd* C, const CoefLayout& L, int kw, int Sm1) {
+  const int Db = L.Db;
+  const long long n_old = (long long)kw * Sm1, n_new = (long long)Db * Sm1;
+  for (long long e = threadIdx.x; e < n_old + n_new; e += blockDim.x) {
+    const bool old = e < n_old;
+    const long long f = old ? e : e - n_old;
+    const int s = (int)(f % Sm1), k = (int)(f / Sm1);
+    const ShiftRef sh{C, s, L.P};
+    if (old) {
+      const zcd d = sh.at(L.o_xinc, Db), c = sh.at(L.o_us, Db);
+      zcd& ub = sh.at(L.o_ub, k);
+      sh.at(L.o_xa, k) += d * ub;
+      ub = c * ub;
+    } else {
+      sh.at(L.o_xa, kw + k) = sh.at(L.o_xinc, k);
+      sh.at(L.o_ub, kw + k) = sh.at(L.o_us, k);
+    }
   }
-  Xd += d * Uc;
-  Uc = c * Uc;
-  for (int q = 0; q < Db; ++q) {
-    sh.at(L.o_xa, kw + q) = sh.at(L.o_xinc, q);
-    sh.at(L.o_ub, kw + q) = sh.at(L.o_us, q);
+  __syncthreads();
+  for (int s = threadIdx.x; s < Sm1; s += blockDim.x) {
+    const ShiftRef sh{C, s, L.P};
+    const zcd d = sh.at(L.o_xinc, Db), c = sh.at(L.o_us, Db);
+    zcd& Uc = sh.at(L.o_scal, SC_UC);
+    sh.at(L.o_scal, SC_XD) += d * Uc;
+    Uc = c * Uc;
   }
-  (void)D;
 }
 
 // y[s][g] (+)= sum_k W[k][g] C[k][s] + carry[s] * Z[s][g], for all shifts s < ns.
-// W: [K][npwx]; C: FP64 [k*P + s]; Z: [s][npwx] (may be null).
+// W: [K][npwx]; C: FP64 [k*P + s]; Z: [s][npwx] (may be null).  The
+// coefficients are staged in shared memory (`smbuf`, room for `smrows` rows of
+// P values; the FFT buffers are idle at this point), in chunks of rows when
+// they do not fit.  In FP32 they are first converted once into `cvt` (global),
+// so no FP64 conversion sits in the inner loop.
+template <typename T>
+struct GemmShape {
+  static constexpr int GL = 128;                        // rows per tile
+  static constexpr int QMAX = sizeof(T) == 4 ? 36 : 16; // shifts per thread per pass
+};
+
 template <typename T>
 __device__ void cta_basis_gemm(cplx<T>* y, long long ldy, bool accumulate, const cplx<T>* W, int K, const zcd* C,
-                               int P, const zcd* carry, const cplx<T>* Z, int ns, int n, int npwx) {
-  constexpr int GL = 128;               // rows per tile
-  constexpr int QMAX = 16;              // shifts per thread per pass
-  const int sgrp = blockDim.x / GL;     // shift groups
+                               int P, const zcd* carry, const cplx<T>* Z, int ns, int n, int npwx, zcd* cvt,
+                               cplx<T>* smbuf, int smrows) {
+  constexpr int GL = GemmShape<T>::GL, QMAX = GemmShape<T>::QMAX;
+  const cplx<T>* Ck;
+  if constexpr (sizeof(T) == 8) {
+    Ck = reinterpret_cast<const cplx<T>*>(C);
+  } else {
+    cplx<T>* c32 = reinterpret_cast<cplx<T>*>(cvt);
+    for (long long e = threadIdx.x; e < (long long)K * P; e += blockDim.x) c32[e] = ccast<T>(C[e]);
+    __syncthreads();
+    Ck = c32;
+  }
+  const int sgrp = blockDim.x / GL;
   const int gl = threadIdx.x % GL, sg = threadIdx.x / GL;
+  const bool whole = K <= smrows;
+  auto fill = [&](int k0, int kc) {
+    __syncthreads();
+    for (int e = threadIdx.x; e < kc * P; e += blockDim.x) smbuf[e] = Ck[(size_t)k0 * P + e];
+    __syncthreads();
+  };
+  if (whole) fill(0, K);
   for (int s0 = 0; s0 < ns; s0 += sgrp * QMAX) {
     for (int g0 = 0; g0 < n; g0 += GL) {
       const int g = g0 + gl;
       cplx<T> acc[QMAX];
 #pragma unroll
       for (int q = 0; q < QMAX; ++q) acc[q] = cplx<T>{0, 0};
-      if (g < n) {
-        for (int k = 0; k < K; ++k) {
-          const cplx<T> w = W[(size_t)k * npwx + g];
-          const zcd* ck = C + (size_t)k * P;
+      for (int k0 = 0; k0 < K; k0 += smrows) {
+        const int kc = min(smrows, K - k0);
+        if (!whole) fill(k0, kc);
+        if (g < n) {
+          for (int kk = 0; kk < kc; ++kk) {
+            const cplx<T> w = W[(size_t)(k0 + kk) * npwx + g];
+            const cplx<T>* ck = smbuf + (size_t)kk * P + s0 + sg;
 #pragma unroll
-          for (int q = 0; q < QMAX; ++q) {
-            const int s = s0 + sg + q * sgrp;
-            if (s < ns) acc[q] += w * ccast<T>(ck[s]);
+            for (int q = 0; q < QMAX; ++q)
+              if (s0 + sg + q * sgrp < ns) cfma(acc[q], w, ck[q * sgrp]);
           }
         }
+      }
+      if (g < n) {
 #pragma unroll
         for (int q = 0; q < QMAX; ++q) {
           const int s = s0 + sg + q * sgrp;
@@ -312,6 +370,7 @@ __device__ void cta_basis_gemm(cplx<T>* y, long long ldy, bool accumulate, const
       }
     }
   }
+  __syncthreads();
 }
 
 // --- the solve of one right-hand side -------------------------------------
@@ -327,6 +386,9 @@ __device__ void solve_one(const SolverArgs<T>& a, const ApplyT& A, int rhs, int 
   const CoefLayout L(l, a.P, a.Kcap);
   const int Db = L.Db;
   const bool explicit_mode = a.mode == 1;
+  int gelems = 0;
+  cplx<T>* gbuf = A.scratch(sm, gelems);
+  const int grows = max(1, gelems / a.P);
   const bool track = Sm1 > 0 && !explicit_mode;
 
   cplx<T>* V = a.ws_vec + (size_t)slot * a.nvec_slot * npwx;
@@ -402,9 +464,9 @@ __device__ void solve_one(const SolverArgs<T>& a, const ApplyT& A, int rhs, int 
     if (track && kw + Db > a.Kcap) {
       // materialise x^sigma and u_0^sigma, start a new window
       cta_basis_gemm<T>(xout + a.ldx, a.ldx, flushed, W, kw, C + L.o_xa, L.P, C + L.o_scal + SC_XD * L.P,
-                        flushed ? U0S : nullptr, Sm1, n, npwx);
+                        flushed ? U0S : nullptr, Sm1, n, npwx, C + L.o_cvt, gbuf, grows);
       cta_basis_gemm<T>(U0S, npwx, false, W, kw, C + L.o_ub, L.P, C + L.o_scal + SC_UC * L.P,
-                        flushed ? U0S : nullptr, Sm1, n, npwx);
+                        flushed ? U0S : nullptr, Sm1, n, npwx, C + L.o_cvt, gbuf, grows);
       __syncthreads();
       for (int s = tid; s < Sm1; s += nt) {
         const ShiftRef sh{C, s, L.P};
@@ -458,12 +520,12 @@ __device__ void solve_one(const SolverArgs<T>& a, const ApplyT& A, int rhs, int 
       if (track)
         for (int q = tid; q < Db; q += nt) cu[(j + 1) * Db + q] = zcd{q == 2 + 2 * j ? 1.0 : 0.0, 0.0};
       alpha = rho / cta_dotu(UV(j + 1), TR0, n, ss.red);
-      for (int s = tid; s < Sm1; s += nt) {
-        const ShiftRef sh{C, s, L.P};
-        shift_bicg_scalars(sh, L, alpha, beta, alpha_old);
-        if (track) replay_bicg1(sh, L, cr, j);
-      }
+      for (int s = tid; s < Sm1; s += nt) shift_bicg_scalars(ShiftRef{C, s, L.P}, L, alpha, beta, alpha_old);
       __syncthreads();
+      if (track) {
+        for (int e = tid; e < L.D * Sm1; e += nt) replay_bicg1_q(ShiftRef{C, e % Sm1, L.P}, L, cr, j, e / Sm1);
+        __syncthreads();
+      }
       if (explicit_mode) {  // L15-L19 on the shift vectors, all shifts at once
         for (long long e = tid; e < (long long)Sm1 * n; e += nt) {
           const int s = (int)(e / n), g = (int)(e - (long long)s * n);
@@ -492,7 +554,7 @@ __device__ void solve_one(const SolverArgs<T>& a, const ApplyT& A, int rhs, int 
       v_axpy(X, alpha, UV(0), n);
       __syncthreads();
       if (track)
-        for (int s = tid; s < Sm1; s += nt) replay_bicg2(ShiftRef{C, s, L.P}, L, cr, j);
+        for (int e = tid; e < L.D * Sm1; e += nt) replay_bicg2_q(ShiftRef{C, e % Sm1, L.P}, L, cr, j, e / Sm1);
       if (explicit_mode)  // L26
         for (long long e = tid; e < (long long)Sm1 * n; e += nt) {
           const int s = (int)(e / n), g = (int)(e - (long long)s * n);
@@ -549,12 +611,12 @@ __device__ void solve_one(const SolverArgs<T>& a, const ApplyT& A, int rhs, int 
         X[g] = x;
         UV(0)[g] = u0;
       }
-      for (int s = tid; s < Sm1; s += nt) {
-        const ShiftRef sh{C, s, L.P};
-        shift_mr_scalars(sh, L, ss);
-        if (track) replay_mr(sh, L, cr, ss);
-      }
+      for (int s = tid; s < Sm1; s += nt) shift_mr_scalars(ShiftRef{C, s, L.P}, L, ss);
       __syncthreads();
+      if (track) {
+        for (int e = tid; e < L.D * Sm1; e += nt) replay_mr_q(ShiftRef{C, e % Sm1, L.P}, L, cr, ss, e / Sm1);
+        __syncthreads();
+      }
       if (explicit_mode) {  // L28-L34
         for (long long e = tid; e < (long long)Sm1 * n; e += nt) {
           const int s = (int)(e / n), g = (int)(e - (long long)s * n);
@@ -578,9 +640,10 @@ __device__ void solve_one(const SolverArgs<T>& a, const ApplyT& A, int rhs, int 
       }
       __syncthreads();
     }
-    if (track)
-      for (int s = tid; s < Sm1; s += nt) replay_window(ShiftRef{C, s, L.P}, L, kw);
-    if (track) kw += Db;
+    if (track) {
+      replay_window_cta(C, L, kw, Sm1);
+      kw += Db;
+    }
     __syncthreads();
     if (conv) break;
     conv = sqrt(cta_nrm2sq(RV(0), n, ss.red)) < a.threshold;
@@ -591,7 +654,7 @@ __device__ void solve_one(const SolverArgs<T>& a, const ApplyT& A, int rhs, int 
   v_copy(xout, X, n);
   if (track)
     cta_basis_gemm<T>(xout + a.ldx, a.ldx, flushed, W, kw, C + L.o_xa, L.P, C + L.o_scal + SC_XD * L.P,
-                      flushed ? U0S : nullptr, Sm1, n, npwx);
+                      flushed ? U0S : nullptr, Sm1, n, npwx, C + L.o_cvt, gbuf, grows);
   if (explicit_mode)
     for (long long e = tid; e < (long long)Sm1 * n; e += nt) {
       const int s = (int)(e / n), g = (int)(e - (long long)s * n);
@@ -625,8 +688,8 @@ __device__ void solve_one(const SolverArgs<T>& a, const ApplyT& A, int rhs, int 
 #undef SCAL
 }
 
-template <typename T, class ApplyT>
-__global__ void __launch_bounds__(kThreads, 1) msbicg_kernel(SolverArgs<T> a, ApplyT A) {
+template <typename T, class ApplyT, int THREADS>
+__global__ void __launch_bounds__(THREADS, 1) msbicg_kernel(SolverArgs<T> a, ApplyT A) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ SeedShared ss;
   __shared__ int s_rhs;

@@ -18,6 +18,7 @@
 #pragma once
 #include "cplx.cuh"
 #include "fft.cuh"
+#include "fftreg.cuh"
 
 namespace sgw {
 
@@ -70,7 +71,7 @@ __device__ __forceinline__ zcd cta_sum(zcd v, zcd* red) {
 template <typename T>
 __device__ zcd cta_dotu(const cplx<T>* x, const cplx<T>* y, int n, zcd* red) {
   cplx<T> p = {0, 0};
-  for (int i = threadIdx.x; i < n; i += blockDim.x) p += x[i] * y[i];
+  for (int i = threadIdx.x; i < n; i += blockDim.x) cfma(p, x[i], y[i]);
   return cta_sum(ccast<double>(p), red);
 }
 
@@ -102,7 +103,7 @@ __device__ void pw_apply_cta(const PwView<T>& op, const int NG, const cplx<T>* _
   for (int i = warp; i < op.nkb + nocc; i += nwarp) {
     const cplx<T>* pr = (i < op.nkb) ? op.vkb + (size_t)i * op.npwx : op.evq + (size_t)(i - op.nkb) * op.npwx;
     cplx<T> acc = {0, 0};
-    for (int g = lane; g < op.npw; g += 32) acc += cmul_conj_a(pr[g], in[g]);
+    for (int g = lane; g < op.npw; g += 32) cfma_conj(acc, pr[g], in[g]);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
       acc.re += __shfl_xor_sync(0xffffffffu, acc.re, o);
@@ -149,8 +150,142 @@ __device__ void pw_apply_cta(const PwView<T>& op, const int NG, const cplx<T>* _
   for (int g = tid; g < op.npw; g += nt) {
     const cplx<T> x = in[g];
     cplx<T> r = op.g2kin[g] * x + sg * x + scale * col[op.g_col[g] * op.ldz + op.g_i3[g]];
-    for (int i = 0; i < op.nkb; ++i) r += op.vkb[(size_t)i * op.npwx + g] * bec[i];
-    for (int v = 0; v < nocc; ++v) r += op.evq[(size_t)v * op.npwx + g] * bec[op.nkb + v];
+    for (int i = 0; i < op.nkb; ++i) cfma(r, op.vkb[(size_t)i * op.npwx + g], bec[i]);
+    for (int v = 0; v < nocc; ++v) cfma(r, op.evq[(size_t)v * op.npwx + g], bec[op.nkb + v]);
+    out[g] = r;
+    if (out2) out2[g] = r;
+  }
+  __syncthreads();
+}
+
+// Line-per-thread variant of pw_apply_cta for box lengths with a register
+// FFT (fftreg.cuh): each thread transforms a whole i3 column, i2 line or i1
+// row in registers.  PF planes are in flight per round; an i1 row is
+// inverse-transformed, multiplied by V_loc(r) and forward-transformed by the
+// same thread, so a plane round needs five CTA barriers instead of a barrier
+// pair per FFT stage.
+template <typename T>
+__device__ void pw_apply_cta_lines(const PwView<T>& op, const int PF, const cplx<T>* __restrict__ in,
+                                   cplx<T>* __restrict__ out, cplx<T>* __restrict__ out2, zcd sigma, cplx<T>* sm,
+                                   cplx<T>* col) {
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const int lane = tid & 31, warp = tid >> 5, nwarp = nt >> 5;
+  const cplx<T>* tw1 = sm;
+  const cplx<T>* tw2 = sm + op.nr1;
+  const cplx<T>* tw3 = sm + op.nr1 + op.nr2;
+  cplx<T>* bec = sm + op.nr1 + op.nr2 + op.nr3;
+  cplx<T>* planes = bec + op.nkb + op.nocc;
+  const int nocc = (op.alpha_pv > 1e-14 || op.alpha_pv < -1e-14) ? op.nocc : 0;  // eps14, linear_op.f90:131
+  const int ldz = op.ldz, pitch = op.pitch, psz = op.nr2 * op.pitch;
+
+  for (int i = warp; i < op.nkb + nocc; i += nwarp) {
+    const cplx<T>* pr = (i < op.nkb) ? op.vkb + (size_t)i * op.npwx : op.evq + (size_t)(i - op.nkb) * op.npwx;
+    cplx<T> acc = {0, 0};
+    for (int g = lane; g < op.npw; g += 32) cfma_conj(acc, pr[g], in[g]);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      acc.re += __shfl_xor_sync(0xffffffffu, acc.re, o);
+      acc.im += __shfl_xor_sync(0xffffffffu, acc.im, o);
+    }
+    if (lane == 0) bec[i] = (i < op.nkb ? op.dvan[i] : (T)op.alpha_pv) * acc;
+  }
+  for (int e = tid; e < op.ncol * ldz; e += nt) col[e] = cplx<T>{0, 0};
+  __syncthreads();
+  for (int g = tid; g < op.npw; g += nt) col[op.g_col[g] * ldz + op.g_i3[g]] = in[g];
+  __syncthreads();
+
+  // Line e of a pass goes to thread e mod blockDim: lines fill whole warps
+  // (a half-empty warp costs the FP64 pipe as much as a full one) and
+  // neighbouring lanes keep neighbouring lines (odd pitches keep their
+  // shared-memory banks apart).
+  auto line_of = [&](int L, int round) {
+    const int e = round * nt + tid;
+    return e < L ? e : -1;
+  };
+  auto rounds_of = [&](int L) { return (L + nt - 1) / nt; };
+  auto zpass = [&](auto NN, auto SS) {
+    constexpr int N = decltype(NN)::value, S = decltype(SS)::value;
+    for (int rd = 0, nr = rounds_of(op.ncol); rd < nr; ++rd) {
+      const int c = line_of(op.ncol, rd);
+      if (c < 0) continue;
+      cplx<T> v[N];
+      cplx<T>* line = col + c * ldz;
+#pragma unroll
+      for (int i = 0; i < N; ++i) v[i] = line[i];
+      fft_reg<T, N, S>(v, tw3);
+#pragma unroll
+      for (int i = 0; i < N; ++i) line[i] = v[i];
+    }
+  };
+  auto ypass = [&](auto NN, auto SS, int np) {
+    constexpr int N = decltype(NN)::value, S = decltype(SS)::value;
+    for (int rd = 0, nr = rounds_of(np * op.ni1); rd < nr; ++rd) {
+      const int e = line_of(np * op.ni1, rd);
+      if (e < 0) continue;
+      const int p = e / op.ni1, l = e - p * op.ni1;
+      cplx<T>* line = planes + p * psz + op.i1_list[l];
+      cplx<T> v[N];
+#pragma unroll
+      for (int i = 0; i < N; ++i) v[i] = line[i * pitch];
+      fft_reg<T, N, S>(v, tw2);
+#pragma unroll
+      for (int i = 0; i < N; ++i) line[i * pitch] = v[i];
+    }
+  };
+  using PLUS = std::integral_constant<int, 1>;
+  using MINUS = std::integral_constant<int, -1>;
+
+  with_len<T>(op.nr3, [&](auto NN) { zpass(NN, PLUS{}); });
+  __syncthreads();
+  for (int p0 = 0; p0 < op.nr3; p0 += PF) {
+    const int np = min(PF, op.nr3 - p0);
+    for (int e = tid; e < np * psz; e += nt) planes[e] = cplx<T>{0, 0};
+    __syncthreads();
+    for (int e = tid; e < np * op.ncol; e += nt) {
+      const int p = e / op.ncol, c = e - p * op.ncol;
+      planes[p * psz + op.col_pos[c]] = col[c * ldz + p0 + p];
+    }
+    __syncthreads();
+    with_len<T>(op.nr2, [&](auto NN) { ypass(NN, PLUS{}, np); });
+    __syncthreads();
+    with_len<T>(op.nr1, [&](auto NN) {
+      constexpr int N = decltype(NN)::value;
+      for (int rd = 0, nr = rounds_of(np * op.nr2); rd < nr; ++rd) {
+        const int e = line_of(np * op.nr2, rd);
+        if (e < 0) continue;
+        const int p = e / op.nr2, i2 = e - p * op.nr2;
+        cplx<T>* row = planes + p * psz + i2 * pitch;
+        const T* vr = op.vrs + ((size_t)(p0 + p) * op.nr2 + i2) * op.nr1;
+        cplx<T> v[N];
+#pragma unroll
+        for (int i = 0; i < N; ++i) v[i] = row[i];
+        fft_reg<T, N, 1>(v, tw1);
+#pragma unroll
+        for (int i = 0; i < N; ++i) v[i] = vr[i] * v[i];
+        fft_reg<T, N, -1>(v, tw1);
+#pragma unroll
+        for (int i = 0; i < N; ++i) row[i] = v[i];
+      }
+    });
+    __syncthreads();
+    with_len<T>(op.nr2, [&](auto NN) { ypass(NN, MINUS{}, np); });
+    __syncthreads();
+    for (int e = tid; e < np * op.ncol; e += nt) {
+      const int p = e / op.ncol, c = e - p * op.ncol;
+      col[c * ldz + p0 + p] = planes[p * psz + op.col_pos[c]];
+    }
+    __syncthreads();
+  }
+  with_len<T>(op.nr3, [&](auto NN) { zpass(NN, MINUS{}); });
+  __syncthreads();
+
+  const T scale = (T)(1.0 / (double)op.nnr);
+  const cplx<T> sg = ccast<T>(sigma);
+  for (int g = tid; g < op.npw; g += nt) {
+    const cplx<T> x = in[g];
+    cplx<T> r = op.g2kin[g] * x + sg * x + scale * col[op.g_col[g] * ldz + op.g_i3[g]];
+    for (int i = 0; i < op.nkb; ++i) cfma(r, op.vkb[(size_t)i * op.npwx + g], bec[i]);
+    for (int v = 0; v < nocc; ++v) cfma(r, op.evq[(size_t)v * op.npwx + g], bec[op.nkb + v]);
     out[g] = r;
     if (out2) out2[g] = r;
   }
@@ -174,7 +309,7 @@ __device__ void dense_apply_cta(const DenseView<T>& op, const cplx<T>* __restric
   for (int row = threadIdx.x; row < op.n; row += blockDim.x) {
     cplx<T> acc = {0, 0};
     const cplx<T>* a = op.a + row;
-    for (int j = 0; j < op.n; ++j) acc += a[(size_t)j * op.n] * sm[j];
+    for (int j = 0; j < op.n; ++j) cfma(acc, a[(size_t)j * op.n], sm[j]);
     acc += sg * sm[row];
     out[row] = acc;
     if (out2) out2[row] = acc;

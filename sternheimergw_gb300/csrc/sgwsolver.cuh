@@ -60,8 +60,8 @@ __device__ void cta_gram_schmidt(int first, int nb, cplx<T>* w, cplx<T>* v, int 
   }
 }
 
-template <typename T, class ApplyT>
-__global__ void __launch_bounds__(kThreads, 1) sgw_solver_kernel(SgwArgs<T> a, ApplyT A) {
+template <typename T, class ApplyT, int THREADS>
+__global__ void __launch_bounds__(THREADS, 1) sgw_solver_kernel(SgwArgs<T> a, ApplyT A) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ zcd red[32];
   __shared__ int flag;
@@ -128,8 +128,8 @@ __global__ void __launch_bounds__(kThreads, 1) sgw_solver_kernel(SgwArgs<T> a, A
 }
 
 // One CTA per vector: ax_i = A(sigma) x_i (the reference's AA callback).
-template <typename T, class ApplyT>
-__global__ void __launch_bounds__(kThreads, 1) apply_kernel(ApplyT A, int m, const cplx<T>* x, long long ldi, cplx<T>* ax,
+template <typename T, class ApplyT, int THREADS>
+__global__ void __launch_bounds__(THREADS, 1) apply_kernel(ApplyT A, int m, const cplx<T>* x, long long ldi, cplx<T>* ax,
                                                             long long ldo, zcd sigma, cplx<T>* col_global,
                                                             long long col_slot) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
