@@ -253,24 +253,63 @@ def time_path(op, bb_d, sg_d, x_d, precision, warmup, steps, l2, name):
                 ierr=ierr.cpu().numpy())
 
 
-def w_error(s, f, bb, x64_d, xm_d):
-    """Relative error of W(G, G'; omega) (all perturbation pairs, every frequency) of the mixed
-    solve against the FP64 solve, normwise per frequency and elementwise."""
+def converged_freqs(op, bb, sigma, x64_d, nfreq, sample=32, tol=1e-6):
+    """Frequencies whose FP64 shifted systems converged: the true relative
+    residual |(A + sigma) x - b| / |b| of the FP64 solution is <= tol at +omega
+    and -omega for every right-hand side of a sample.  The reference tests only
+    the seed residual (bicgstab.f90:237,245), so shifted systems far from the
+    seed may stop unconverged; their W is not defined by either solver."""
+    S = sigma.shape[1]
+    worst = np.zeros(S)
+    for r in range(0, bb.shape[0], max(1, bb.shape[0] // sample)):
+        x = x64_d[r].cpu().numpy()
+        for k in range(S):
+            res = op.apply(sigma[r, k], x[k]) - bb[r]
+            worst[k] = max(worst[k], np.linalg.norm(res) / np.linalg.norm(bb[r]))
+    ok = []
+    for fi in range(nfreq):
+        minus = (nfreq + fi - 1) if S == 2 * nfreq - 1 else nfreq + fi
+        ok.append(worst[fi] <= tol and (fi == 0 and S == 2 * nfreq - 1 or worst[minus] <= tol))
+    return np.array(ok), worst
+
+
+def shift_error(x64_d, xm_d, worst, tol=1e-6):
+    """Largest relative difference |x_mixed - x_fp64| / |x_fp64| over the shifts
+    whose FP64 solution converged (true relative residual <= tol on the sample)."""
+    ok = np.nonzero(worst <= tol)[0]
+    if ok.size == 0:
+        return None, 0
     import torch
-    from sternheimergw_gb300 import linter
+    idx = torch.as_tensor(ok, device="cuda")
+    a, b = xm_d[:, idx], x64_d[:, idx]
+    err = (torch.linalg.vector_norm(a - b, dim=2) / torch.linalg.vector_norm(b, dim=2)).max().item()
+    return err, int(ok.size)
+
+
+def w_error_imag_axis():
+    """W(G, G'; omega) error of the mixed solve against FP64 on the imaginary-axis
+    system (fcc, 20^3, 8 perturbations, 16 frequencies i*[0..50] eV, 4 bands),
+    where every shifted system converges: normwise max over frequencies and
+    elementwise max over |W| >= 1e-3 max |W|."""
+    import sternheimergw_gb300 as sg
+    from sternheimergw_gb300 import linter, synth
+    s, f = synth.config("c4")
+    op = sg.PlaneWaveOperator(s)
     npert, nocc = len(s["gpert"]), s["nocc"]
-    S = x64_d.shape[1]
-    B = torch.from_numpy(bb.reshape(npert, nocc, -1)).cuda()
+    B = np.stack([linter.coulomb_rhs(s, ip) for ip in range(npert)])
+    sh = np.tile(linter.coulomb_shifts(s, f), (npert, 1))
+    bb = B.reshape(npert * nocc, -1)
+    x64, e64, _ = sg.solve_batch(op, bb, sh, threshold=THRESHOLD)
+    xm, em, _ = sg.solve_batch(op, bb, sh, threshold=THRESHOLD, precision=1)
+    S = sh.shape[1]
     v = linter.coulomb_v(s)
-    W = []
-    for x in (x64_d, xm_d):
-        chi = linter.chi_matrix(B, x.view(npert, nocc, S, -1), f)
-        W.append(linter.w_from_chi(chi, v))
-    d = W[1] - W[0]
-    norm = (torch.linalg.matrix_norm(d) / torch.linalg.matrix_norm(W[0])).max().item()
-    big = W[0].abs() >= 1e-3 * W[0].abs().amax(dim=(1, 2), keepdim=True)
-    elem = (d.abs() / W[0].abs())[big].max().item()
-    return norm, elem
+    W64 = linter.w_from_chi(linter.chi_matrix(B, x64.reshape(npert, nocc, S, -1), f), v)
+    WM = linter.w_from_chi(linter.chi_matrix(B, xm.reshape(npert, nocc, S, -1), f), v)
+    d = WM - W64
+    norm = float(np.max(np.linalg.norm(d, axis=(1, 2)) / np.linalg.norm(W64, axis=(1, 2))))
+    big = np.abs(W64) >= 1e-3 * np.abs(W64).max(axis=(1, 2), keepdims=True)
+    elem = float(np.max((np.abs(d) / np.abs(W64))[big]))
+    return norm, elem, int(max(e64.max(), em.max()))
 
 
 def run_gpu(args, rank, world):
@@ -326,7 +365,9 @@ def run_gpu(args, rank, world):
     solves = nrhs * S
     value = world * solves / (ms_m * 1e-3)
     value64 = world * solves / (ms_64 * 1e-3)
-    w_norm, w_elem = w_error(s, f, bb, x64_d, xm_d)
+    freq_ok, worst = converged_freqs(op, bb, sigma, x64_d, len(f))
+    x_err, n_conv_shifts = shift_error(x64_d, xm_d, worst)
+    w_norm, w_elem, w_ierr = w_error_imag_axis()
 
     # end to end through the C ABI with pinned host buffers (mixed precision, the headline path)
     bb_h = torch.from_numpy(bb).pin_memory()
@@ -368,9 +409,15 @@ def run_gpu(args, rank, world):
             "plain_fp64": {"value": value64, "unit": "solves/s", "ms_per_step": ms_64,
                            "ierr_max": int(p64["ierr"].max())},
             "speedup_mixed_vs_fp64": value / value64,
-            "w_err": {"normwise_max_over_freq": w_norm, "elementwise_max": w_elem,
-                      "elements": "W(G,G';omega) over 113x113 perturbations x 35 frequencies, |W|>=1e-3 max",
-                      "ok": bool(w_norm <= 1e-6), "mixed_ierr_max": int(pm["ierr"].max())},
+            "w_err": {"normwise_max_over_freq": w_norm, "elementwise_max": w_elem, "ierr_max": w_ierr,
+                      "system": "imaginary-axis system (fcc 20^3, 8 perturbations x 16 frequencies i[0,50] eV), "
+                                "every shifted system converged; mixed vs FP64",
+                      "ok": bool(w_norm <= 1e-6)},
+            "shift_err_workload": {"max_rel_x_err": x_err, "converged_shifts": n_conv_shifts, "shifts": S,
+                                   "converged_freq_pairs": int(np.sum(freq_ok)),
+                                   "note": "real-axis frequencies: with seed-only convergence (the reference's rule) "
+                                           "only shifts near the seed converge, so W is undefined here; the error "
+                                           "of mixed vs FP64 is taken over the converged shifts"},
             "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h), "ms_per_step": float(np.median(e2e_ms))},
             "roofline": {"bound": "fp32", "achieved": ach32, "peak": peak32, "unit": "TFLOP/s",

@@ -449,10 +449,8 @@ __device__ void solve_one(const SolverArgs<T>& a, const ApplyT& A, int rhs, int 
         sh.at(L.o_mu, SGW_MUIDX(jj, ii)) = binom * p;
       }
     }
-    for (int k = 0; k < a.Kcap; ++k) {
-      sh.at(L.o_xa, k) = zcd{0.0, 0.0};
-      sh.at(L.o_ub, k) = zcd{0.0, 0.0};
-    }
+    // the window rows XA, UB need no clearing: replay_window_cta writes row kw+q
+    // before any later iteration reads it
   }
   __syncthreads();
 
@@ -468,12 +466,8 @@ __device__ void solve_one(const SolverArgs<T>& a, const ApplyT& A, int rhs, int 
       cta_basis_gemm<T>(U0S, npwx, false, W, kw, C + L.o_ub, L.P, C + L.o_scal + SC_UC * L.P,
                         flushed ? U0S : nullptr, Sm1, n, npwx, C + L.o_cvt, gbuf, grows);
       __syncthreads();
-      for (int s = tid; s < Sm1; s += nt) {
+      for (int s = tid; s < Sm1; s += nt) {  // new window: rows are rewritten before they are read
         const ShiftRef sh{C, s, L.P};
-        for (int k = 0; k < kw; ++k) {
-          sh.at(L.o_xa, k) = zcd{0.0, 0.0};
-          sh.at(L.o_ub, k) = zcd{0.0, 0.0};
-        }
         sh.at(L.o_scal, SC_UC) = zcd{1.0, 0.0};
         sh.at(L.o_scal, SC_XD) = zcd{0.0, 0.0};
       }
