@@ -43,19 +43,28 @@ def log(*a):
     print(*a, file=sys.stderr, flush=True)
 
 
-def make_workload():
+def make_workload(op=None):
+    """The large-system workload: right-hand sides of every (perturbation, band)
+    and the shift lists.  With an operator handle the right-hand sides are built
+    on the GPU (sgw_coulomb_rhs) and returned as a CUDA tensor too; without one
+    (the CPU reference arm) the oracle's numpy restatement builds them."""
     from sternheimergw_gb300 import linter, synth
     t = time.time()
     s, f = synth.config("c1")
     nocc = s["nocc"]
     npert = len(s["gpert"])
-    bb = np.zeros((npert * nocc, s["npw"]), dtype=np.complex128)
-    for ip in range(npert):
-        bb[ip * nocc:(ip + 1) * nocc] = linter.coulomb_rhs(s, ip)
     sh1 = linter.coulomb_shifts(s, f)
     sigma = np.tile(sh1, (npert, 1))
+    if op is None:
+        from oracle import linter_ref
+        bb = np.concatenate([linter_ref.coulomb_rhs(s, ip) for ip in range(npert)])
+        bb_d = None
+    else:
+        op = op(s) if callable(op) else op
+        bb_d = linter.coulomb_rhs(op, s, device=True)
+        bb = bb_d.cpu().numpy()
     log(f"[bench] workload built in {time.time() - t:.1f}s: nrhs={bb.shape[0]} S={sigma.shape[1]} npw={s['npw']}")
-    return s, f, bb, sigma
+    return s, f, bb, sigma, bb_d
 
 
 # --- algorithmic FP64 work of one solve --------------------------------------
@@ -185,7 +194,7 @@ def cpu_reference(s, bb, sigma, sample, threads):
 def run_reference(args, rank, world):
     if rank != 0:
         return
-    s, f, bb, sigma = make_workload()
+    s, f, bb, sigma, _ = make_workload()
     threads = os.cpu_count() or 1
     sample = min(bb.shape[0], 32 * threads)
     vals = []  # the CPU path has nothing to warm up; every step is timed
@@ -296,15 +305,13 @@ def w_error_imag_axis():
     s, f = synth.config("c4")
     op = sg.PlaneWaveOperator(s)
     npert, nocc = len(s["gpert"]), s["nocc"]
-    B = np.stack([linter.coulomb_rhs(s, ip) for ip in range(npert)])
+    bb = linter.coulomb_rhs(op, s)
     sh = np.tile(linter.coulomb_shifts(s, f), (npert, 1))
-    bb = B.reshape(npert * nocc, -1)
     x64, e64, _ = sg.solve_batch(op, bb, sh, threshold=THRESHOLD)
     xm, em, _ = sg.solve_batch(op, bb, sh, threshold=THRESHOLD, precision=1)
-    S = sh.shape[1]
     v = linter.coulomb_v(s)
-    W64 = linter.w_from_chi(linter.chi_matrix(B, x64.reshape(npert, nocc, S, -1), f), v)
-    WM = linter.w_from_chi(linter.chi_matrix(B, xm.reshape(npert, nocc, S, -1), f), v)
+    W64 = linter.w_from_chi(linter.chi_matrix(op, bb, x64, nocc, f), v)
+    WM = linter.w_from_chi(linter.chi_matrix(op, bb, xm, nocc, f), v)
     d = WM - W64
     norm = float(np.max(np.linalg.norm(d, axis=(1, 2)) / np.linalg.norm(W64, axis=(1, 2))))
     big = np.abs(W64) >= 1e-3 * np.abs(W64).max(axis=(1, 2), keepdims=True)
@@ -322,13 +329,19 @@ def run_gpu(args, rank, world):
     dev = int(os.environ.get("LOCAL_RANK", 0))
     torch.cuda.set_device(dev)
     _capi.lib(build_if_missing=False)
-    s, f, bb, sigma = make_workload()
+    holder = {}
+
+    def make_op(system):
+        holder["op"] = sg.PlaneWaveOperator(system)
+        return holder["op"]
+
+    s, f, bb, sigma, bb_d = make_workload(make_op)
+    op = holder["op"]
+    rhs_ms = op.kernel_timing(3)[0]
     if args.nrhs:
-        bb, sigma = bb[:args.nrhs], sigma[:args.nrhs]
+        bb, sigma, bb_d = bb[:args.nrhs], sigma[:args.nrhs], bb_d[:args.nrhs].contiguous()
     nrhs, S = sigma.shape
     n = s["npw"]
-    op = sg.PlaneWaveOperator(s)
-    bb_d = torch.from_numpy(bb).cuda()
     sg_d = torch.from_numpy(sigma).cuda()
     x64_d = torch.empty((nrhs, S, n), dtype=torch.complex128, device="cuda")
     xm_d = torch.empty((nrhs, S, n), dtype=torch.complex128, device="cuda")
@@ -368,6 +381,19 @@ def run_gpu(args, rank, world):
     freq_ok, worst = converged_freqs(op, bb, sigma, x64_d, len(f))
     x_err, n_conv_shifts = shift_error(x64_d, xm_d, worst)
     w_norm, w_elem, w_ierr = w_error_imag_axis()
+
+    # density response of the whole workload from the mixed solutions (sgw_chi, FP64, +-omega average fused)
+    from sternheimergw_gb300 import linter
+    nocc = s["nocc"]
+    chi_ms = chi_flops = None
+    if nrhs % nocc == 0:
+        chi_times = []
+        for _ in range(4):
+            flush_l2(l2)
+            linter.chi_matrix(op, bb_d, xm_d, nocc, f)
+            chi_times.append(op.kernel_timing(4)[0])
+        chi_ms = float(np.median(chi_times[1:]))
+        chi_flops = 8.0 * (nrhs // nocc) * len(s["gpert"]) * nocc * n * len(f)
 
     # end to end through the C ABI with pinned host buffers (mixed precision, the headline path)
     bb_h = torch.from_numpy(bb).pin_memory()
@@ -429,6 +455,14 @@ def run_gpu(args, rank, world):
                               "frac": ach64 / peak64, "traffic": None, "kernel": "msbicg_kernel<double>",
                               "ms_per_launch": k64_ms / max(k64_n, 1), "flops_per_launch": f64,
                               "peak_source": "in-run cuBLAS DGEMM 8192^3 (MEASURED_PEAKS.json has no FP64 figure)"},
+            "caller_kernels": {
+                "rhs_build_ms": rhs_ms, "rhs_built": int(len(s["gpert"]) * nocc),
+                "chi_ms": chi_ms, "chi_flops": chi_flops,
+                "chi_tflops": (chi_flops / (chi_ms * 1e-3) / 1e12) if chi_ms else None,
+                "chi_frac_of_fp64_peak": (chi_flops / (chi_ms * 1e-3) / 1e12 / peak64) if chi_ms else None,
+                "note": "rhs: sgw_coulomb_rhs for every (perturbation, band) of the workload, host copies "
+                        "excluded; chi: sgw_chi over all solutions (FP64 complex contraction, +-omega "
+                        "average fused), timed outside the solve steps"},
             "mixed_kernel_ms_per_step": {"fp32_solve": k32_ms / args.steps, "fp64_seed_residual": kres_ms / args.steps,
                                          "total": ms_m},
             "cpu_baseline": {"value": cpu_v, "unit": "solves/s", "cores": os.cpu_count() or 1, "kind": "port",

@@ -168,6 +168,66 @@ sgw_status sgw_solve_batch(sgw_operator* op, const sgw_batch_desc* desc);
  * (cudaGetSymbolAddress); make it before any stream capture. */
 sgw_status sgw_solve_batch_noalloc(sgw_operator* op, const sgw_batch_desc* desc);
 
+/* Right-hand sides of the Coulomb solve, b_(p,v) = -P_c^+ (Delta V_p psi_v),
+ * on the handle's k+q sphere (the operator's nl map and occupied states evq).
+ * Replaces dvqpsi_us (dvqpsi_us.f90:25-143, the box product at :96-132) and
+ * QE's orthogonalize as called at solve_linter.f90:331-337, for every band
+ * and every perturbation in one call.  Plane-wave operators only.
+ *   nl_k[npw_k]        box index (0-based, i1 + nr1 (i2 + nr2 i3)) of each
+ *                      k-sphere plane wave (the igk_k map of dvqpsi_us.f90:104)
+ *   evc[v*ldk + g]     psi_v at k, v < the operator's nbnd_occ
+ *   dvbare[p*lddv + r] Delta V_p(r) on the box, p < npert
+ *   bb[(p*nbnd_occ + v)*ldb + g]   output on the k+q sphere, g < npw
+ * memory 0: host pointers (copies inside the call); 1: device pointers. */
+typedef struct sgw_rhs_desc {
+  int32_t npert;
+  int32_t npw_k;
+  const int32_t* nl_k;
+  const sgw_zcomplex* evc;
+  int64_t ldk;
+  const sgw_zcomplex* dvbare;
+  int64_t lddv;
+  sgw_zcomplex* bb;
+  int64_t ldb;
+  int32_t memory;
+} sgw_rhs_desc;
+
+sgw_status sgw_coulomb_rhs(sgw_operator* op, const sgw_rhs_desc* desc);
+
+/* Density response on the perturbation set from the solved batch, with the
+ * +-omega average of solve_linter.f90:462-480 fused in:
+ *   chi[(q*nfreq + f)*ldc + p] = -weight * sum_v <b_(p,v) | xbar_(q,v,f)>
+ *   xbar_f = x(shift_plus[f])                       if shift_minus[f] < 0
+ *          = (x(shift_plus[f]) + x(shift_minus[f])) / 2   otherwise
+ * with bb[(p*nbnd + v)*ldb + g] the right-hand sides and
+ * xx[(q*nbnd + v)*ldr + s*ldx + g] the solutions of sgw_solve_batch.  The
+ * layout of chi is that of scrcoul(ig', f, task) (coulomb.f90:146-151): one
+ * column over the bra perturbations p per (frequency, solved perturbation q).
+ * Stands for incdrhoscf at solve_linter.f90:489-497 followed by the fwfft and
+ * the pick of the G' components (coulomb.f90:146-151), projected on the
+ * perturbation set.  shift_plus/shift_minus are host arrays; the other
+ * pointers follow `memory` (0 host, 1 device).  FP64. */
+typedef struct sgw_chi_desc {
+  int32_t npert_b;
+  int32_t npert_x;
+  int32_t nbnd;
+  int32_t npw;
+  const sgw_zcomplex* bb;
+  int64_t ldb;
+  const sgw_zcomplex* xx;
+  int64_t ldx;
+  int64_t ldr;
+  int32_t nfreq;
+  const int32_t* shift_plus;
+  const int32_t* shift_minus;
+  double weight;
+  sgw_zcomplex* chi;
+  int64_t ldc;
+  int32_t memory;
+} sgw_chi_desc;
+
+sgw_status sgw_chi(sgw_operator* op, const sgw_chi_desc* desc);
+
 /* Device time (ms) of the last solve on this handle's stream, measured with
  * CUDA events around the kernels; and the number of kernel launches it used. */
 sgw_status sgw_last_timing(sgw_operator* op, double* ms, int64_t* launches);
@@ -175,7 +235,8 @@ sgw_status sgw_last_timing(sgw_operator* op, double* ms, int64_t* launches);
 /* Device time (ms, CUDA events on the handle's stream) and launch count of
  * one kernel in the last sgw_solve_batch call: kernel 0 = FP64 multishift
  * solve, 1 = FP32 multishift solve (mixed precision), 2 = FP64 seed residual
- * (mixed precision). */
+ * (mixed precision); kernel 3 = the last sgw_coulomb_rhs (both of its
+ * kernels), 4 = the last sgw_chi. */
 sgw_status sgw_kernel_timing(sgw_operator* op, int32_t kernel, double* ms, int64_t* launches);
 
 /* One-line description of the last error on this thread. */

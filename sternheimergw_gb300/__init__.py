@@ -7,7 +7,9 @@ solver call does, and raises if it is missing.
 from .solver import (BICGSTAB_MULTI, BICGSTAB_NO_MULTI, SGW_LINEAR_SOLVER, BicgstabConfig, DenseOperator,
                      LinearSolverConfig, PlaneWaveOperator, SelectSolverConfig, bicgstab, linear_solver,
                      select_solver, solve_batch)
+from ._capi import SgwError
+from . import solver
 
 __all__ = ["BICGSTAB_MULTI", "BICGSTAB_NO_MULTI", "SGW_LINEAR_SOLVER", "BicgstabConfig", "DenseOperator",
            "LinearSolverConfig", "PlaneWaveOperator", "SelectSolverConfig", "bicgstab", "linear_solver",
-           "select_solver", "solve_batch"]
+           "select_solver", "solve_batch", "SgwError", "solver"]

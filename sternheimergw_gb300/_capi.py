@@ -38,6 +38,19 @@ class BatchDesc(C.Structure):
                 ("iters", C.c_void_p)]
 
 
+class RhsDesc(C.Structure):
+    _fields_ = [("npert", C.c_int32), ("npw_k", C.c_int32), ("nl_k", C.c_void_p), ("evc", C.c_void_p),
+                ("ldk", C.c_int64), ("dvbare", C.c_void_p), ("lddv", C.c_int64), ("bb", C.c_void_p),
+                ("ldb", C.c_int64), ("memory", C.c_int32)]
+
+
+class ChiDesc(C.Structure):
+    _fields_ = [("npert_b", C.c_int32), ("npert_x", C.c_int32), ("nbnd", C.c_int32), ("npw", C.c_int32),
+                ("bb", C.c_void_p), ("ldb", C.c_int64), ("xx", C.c_void_p), ("ldx", C.c_int64), ("ldr", C.c_int64),
+                ("nfreq", C.c_int32), ("shift_plus", C.c_void_p), ("shift_minus", C.c_void_p),
+                ("weight", C.c_double), ("chi", C.c_void_p), ("ldc", C.c_int64), ("memory", C.c_int32)]
+
+
 # (name, restype, argtypes) of every entry point declared in include/sgw_capi.h
 SIGNATURES = [
     ("sgw_operator_create_pw", C.c_int, [C.POINTER(PwOperatorDesc), C.POINTER(C.c_void_p)]),
@@ -53,6 +66,8 @@ SIGNATURES = [
                                     C.c_void_p, C.c_int64, C.POINTER(C.c_int32)]),
     ("sgw_solve_batch", C.c_int, [C.c_void_p, C.POINTER(BatchDesc)]),
     ("sgw_solve_batch_noalloc", C.c_int, [C.c_void_p, C.POINTER(BatchDesc)]),
+    ("sgw_coulomb_rhs", C.c_int, [C.c_void_p, C.POINTER(RhsDesc)]),
+    ("sgw_chi", C.c_int, [C.c_void_p, C.POINTER(ChiDesc)]),
     ("sgw_last_timing", C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_int64)]),
     ("sgw_kernel_timing", C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_int64)]),
     ("sgw_last_error", C.c_char_p, []),

@@ -112,13 +112,15 @@ static sgw_status init_common(sgw_operator* op) {
   SGW_CK(cudaStreamCreateWithFlags(&op->stream, cudaStreamNonBlocking));
   SGW_CK(cudaEventCreate(&op->ev0));
   SGW_CK(cudaEventCreate(&op->ev1));
+  SGW_CK(cudaEventCreate(&op->lev0));
+  SGW_CK(cudaEventCreate(&op->lev1));
   for (int i = 0; i < 2 * kMaxTimedLaunches; ++i) SGW_CK(cudaEventCreate(&op->kev[i]));
   return SGW_OK;
 }
 
 // Sum the per-kernel event pairs of the finished solve (stream already synchronised).
 static void collect_kernel_times(sgw_operator* op) {
-  for (int k = 0; k < K_NUM; ++k) {
+  for (int k = 0; k < K_RHS; ++k) {  // the solve kernels; rhs and chi keep their own
     op->kernel_ms[k] = 0.0;
     op->kernel_launches[k] = 0;
   }
@@ -256,6 +258,10 @@ static sgw_status create_pw(const sgw_pw_operator_desc* d, sgw_operator** out) {
   op->npwx = (d->npw + 31) / 32 * 32;
   op->alpha_pv = d->alpha_pv;
   sgw_status s = init_common(op);
+  if (s == SGW_OK) {
+    std::vector<int> nl(d->nl, d->nl + d->npw);
+    s = op->nlkq.upload(nl.data(), nl.size());
+  }
   if (s == SGW_OK) s = op->gcol.upload(gcol.data(), gcol.size());
   if (s == SGW_OK) s = op->gi3.upload(gi3.data(), gi3.size());
   if (s == SGW_OK) s = op->colpos.upload(colpos.data(), colpos.size());
@@ -525,12 +531,16 @@ sgw_status sgw_operator_destroy(sgw_operator* op) {
                     &op->vkb64, &op->vkb32, &op->dvan64, &op->dvan32, &op->evq64, &op->evq32, &op->tw64, &op->tw32,
                     &op->a64, &op->a32, &op->ws64.vec, &op->ws64.coef, &op->ws64.col, &op->ws64.counter,
                     &op->ws32.vec, &op->ws32.coef, &op->ws32.col, &op->ws32.counter, &op->st_bb, &op->st_sigma,
-                    &op->st_xx, &op->st_ierr, &op->st_iters, &op->st_misc, &op->st_misc2, &op->st_misc3};
+                    &op->st_xx, &op->st_ierr, &op->st_iters, &op->st_misc, &op->st_misc2, &op->st_misc3,
+                    &op->nlkq, &op->lt_psi, &op->lt_box, &op->lt_nlk, &op->lt_evc, &op->lt_dv, &op->lt_bb,
+                    &op->lt_flag, &op->lt_part, &op->lt_sidx, &op->lt_xx, &op->lt_chi};
   for (DevBuf* b : bufs) b->release();
   for (int i = 0; i < 2 * kMaxTimedLaunches; ++i)
     if (op->kev[i]) cudaEventDestroy(op->kev[i]);
   if (op->ev0) cudaEventDestroy(op->ev0);
   if (op->ev1) cudaEventDestroy(op->ev1);
+  if (op->lev0) cudaEventDestroy(op->lev0);
+  if (op->lev1) cudaEventDestroy(op->lev1);
   if (op->stream) cudaStreamDestroy(op->stream);
   delete op;
   return SGW_OK;

@@ -85,7 +85,7 @@ struct Workspace {
 };
 
 // Kernel kinds timed with CUDA events on the operator's stream.
-enum KernelKind { K_MSBICG_F64 = 0, K_MSBICG_F32 = 1, K_RESIDUAL_F64 = 2, K_NUM = 3 };
+enum KernelKind { K_MSBICG_F64 = 0, K_MSBICG_F32 = 1, K_RESIDUAL_F64 = 2, K_RHS = 3, K_CHI = 4, K_NUM = 5 };
 constexpr int kMaxTimedLaunches = 64;
 
 }  // namespace sgw
@@ -97,6 +97,7 @@ struct sgw_operator {
   size_t smem_optin = 0;
   cudaStream_t stream = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  cudaEvent_t lev0 = nullptr, lev1 = nullptr;  // sgw_coulomb_rhs / sgw_chi timing
   double last_ms = 0.0;
   long long last_launches = 0;
   // per-kernel timing of the last solve: event pairs recorded around launches
@@ -107,7 +108,7 @@ struct sgw_operator {
   long long kernel_launches[sgw::K_NUM] = {};
   double alpha_pv = 0.0;
   // tables
-  sgw::DevBuf gcol, gi3, colpos, i1list, g2k64, g2k32, vrs64, vrs32, vkb64, vkb32, dvan64, dvan32, evq64, evq32,
+  sgw::DevBuf nlkq, gcol, gi3, colpos, i1list, g2k64, g2k32, vrs64, vrs32, vkb64, vkb32, dvan64, dvan32, evq64, evq32,
       tw64, tw32, a64, a32;
   sgw::PwView<double> pw64{};
   sgw::PwView<float> pw32{};
@@ -117,6 +118,8 @@ struct sgw_operator {
   // workspaces and staging
   sgw::Workspace ws64, ws32;
   sgw::DevBuf st_bb, st_sigma, st_xx, st_ierr, st_iters, st_misc, st_misc2, st_misc3;
+  // right-hand-side build and chi accumulation
+  sgw::DevBuf lt_psi, lt_box, lt_nlk, lt_evc, lt_dv, lt_bb, lt_flag, lt_part, lt_sidx, lt_xx, lt_chi;
 };
 
 namespace sgw {

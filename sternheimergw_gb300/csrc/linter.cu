@@ -1,0 +1,209 @@
+// C-ABI of the caller-side kernels around the solve: the Coulomb right-hand
+// sides (dvqpsi_us + orthogonalize, rhs.cuh) and the density response with
+// the +-omega average (chi.cuh).
+#include <algorithm>
+#include <string>
+#include <vector>
+
+#include "chi.cuh"
+#include "host.cuh"
+#include "rhs.cuh"
+
+namespace sgw {
+
+static sgw_status lt_arg_error(const std::string& msg) {
+  set_error(msg);
+  return SGW_ERR_ARG;
+}
+
+static sgw_status coulomb_rhs(sgw_operator* op, const sgw_rhs_desc* d) {
+  if (!op || !d) return lt_arg_error("null argument");
+  if (op->kind != 1) return lt_arg_error("sgw_coulomb_rhs needs a plane-wave operator");
+  const PwView<double>& v = op->pw64;
+  const int nocc = v.nocc, npw = v.npw;
+  const long long nnr = v.nnr;
+  if (d->npert < 0 || d->npw_k < 0 || d->memory < 0 || d->memory > 1) return lt_arg_error("invalid rhs description");
+  if (d->npert == 0 || nocc == 0) return SGW_OK;
+  if (!d->nl_k || !d->evc || !d->dvbare || !d->bb) return lt_arg_error("null rhs array");
+  if (d->ldk < d->npw_k || d->lddv < nnr || d->ldb < npw) return lt_arg_error("leading dimensions too small");
+  const int nslot = std::min(d->npert * nocc, op->num_sms);
+  sgw_status s;
+  if ((s = op->lt_psi.ensure(sizeof(zcd) * nocc * nnr)) != SGW_OK) return s;
+  if ((s = op->lt_box.ensure(sizeof(zcd) * nslot * nnr)) != SGW_OK) return s;
+  if ((s = op->lt_flag.ensure(sizeof(int))) != SGW_OK) return s;
+  RhsArgs a{};
+  a.npert = d->npert;
+  a.nocc = nocc;
+  a.npw_k = d->npw_k;
+  a.npw = npw;
+  a.npwx = v.npwx;
+  a.nr1 = v.nr1;
+  a.nr2 = v.nr2;
+  a.nr3 = v.nr3;
+  a.nl = op->nlkq.as<int>();
+  a.evq = v.evq;
+  a.psi_r = op->lt_psi.as<zcd>();
+  a.box = op->lt_box.as<zcd>();
+  a.bad_index = op->lt_flag.as<int>();
+  a.p1 = v.p1;
+  a.p2 = v.p2;
+  a.p3 = v.p3;
+  a.tw = v.tw;
+  SGW_CK(cudaMemsetAsync(a.bad_index, 0, sizeof(int), op->stream));
+  if (d->memory == 0) {
+    for (int g = 0; g < d->npw_k; ++g)
+      if (d->nl_k[g] < 0 || d->nl_k[g] >= nnr) return lt_arg_error("nl_k index outside the FFT box");
+    if ((s = op->lt_nlk.ensure(sizeof(int) * std::max(d->npw_k, 1))) != SGW_OK) return s;
+    if ((s = op->lt_evc.ensure(sizeof(zcd) * (size_t)nocc * std::max(d->npw_k, 1))) != SGW_OK) return s;
+    if ((s = op->lt_dv.ensure(sizeof(zcd) * (size_t)d->npert * nnr)) != SGW_OK) return s;
+    if ((s = op->lt_bb.ensure(sizeof(zcd) * (size_t)d->npert * nocc * npw)) != SGW_OK) return s;
+    SGW_CK(cudaEventRecord(op->lev0, op->stream));
+    SGW_CK(cudaMemcpyAsync(op->lt_nlk.p, d->nl_k, sizeof(int) * d->npw_k, cudaMemcpyHostToDevice, op->stream));
+    SGW_CK(cudaMemcpy2DAsync(op->lt_evc.p, sizeof(zcd) * d->npw_k, d->evc, sizeof(zcd) * d->ldk,
+                             sizeof(zcd) * d->npw_k, nocc, cudaMemcpyHostToDevice, op->stream));
+    SGW_CK(cudaMemcpy2DAsync(op->lt_dv.p, sizeof(zcd) * nnr, d->dvbare, sizeof(zcd) * d->lddv, sizeof(zcd) * nnr,
+                             d->npert, cudaMemcpyHostToDevice, op->stream));
+    a.nl_k = op->lt_nlk.as<int>();
+    a.evc = op->lt_evc.as<zcd>();
+    a.ldk = d->npw_k;
+    a.dv = op->lt_dv.as<zcd>();
+    a.lddv = nnr;
+    a.bb = op->lt_bb.as<zcd>();
+    a.ldb = npw;
+  } else {
+    SGW_CK(cudaEventRecord(op->lev0, op->stream));
+    a.nl_k = d->nl_k;
+    a.evc = reinterpret_cast<const zcd*>(d->evc);
+    a.ldk = d->ldk;
+    a.dv = reinterpret_cast<const zcd*>(d->dvbare);
+    a.lddv = d->lddv;
+    a.bb = reinterpret_cast<zcd*>(d->bb);
+    a.ldb = d->ldb;
+  }
+  const size_t tw_bytes = sizeof(zcd) * (v.nr1 + v.nr2 + v.nr3);
+  rhs_psi_kernel<<<nocc, 256, tw_bytes, op->stream>>>(a);
+  SGW_CK(cudaGetLastError());
+  rhs_kernel<<<nslot, 256, tw_bytes + sizeof(zcd) * nocc, op->stream>>>(a);
+  SGW_CK(cudaGetLastError());
+  if (d->memory == 0)
+    SGW_CK(cudaMemcpy2DAsync(d->bb, sizeof(zcd) * d->ldb, a.bb, sizeof(zcd) * npw, sizeof(zcd) * npw,
+                             (size_t)d->npert * nocc, cudaMemcpyDeviceToHost, op->stream));
+  SGW_CK(cudaEventRecord(op->lev1, op->stream));
+  int bad = 0;
+  SGW_CK(cudaMemcpyAsync(&bad, a.bad_index, sizeof(int), cudaMemcpyDeviceToHost, op->stream));
+  SGW_CK(cudaStreamSynchronize(op->stream));
+  float ms = 0.f;
+  SGW_CK(cudaEventElapsedTime(&ms, op->lev0, op->lev1));
+  op->kernel_ms[K_RHS] = ms;
+  op->kernel_launches[K_RHS] = 2;
+  if (bad) return lt_arg_error("nl_k index outside the FFT box");
+  return SGW_OK;
+}
+
+static sgw_status chi(sgw_operator* op, const sgw_chi_desc* d) {
+  if (!op || !d) return lt_arg_error("null argument");
+  if (d->npert_b < 0 || d->npert_x < 0 || d->nbnd < 0 || d->npw < 1 || d->nfreq < 0 || d->memory < 0 ||
+      d->memory > 1)
+    return lt_arg_error("invalid chi description");
+  const int P = d->npert_b, Q = d->npert_x, F = d->nfreq;
+  if (P == 0 || Q == 0 || F == 0) return SGW_OK;
+  if (!d->bb || !d->xx || !d->chi || !d->shift_plus || !d->shift_minus) return lt_arg_error("null chi array");
+  if (d->ldb < d->npw || d->ldx < d->npw || d->ldc < P) return lt_arg_error("leading dimensions too small");
+  int smax = 0;
+  for (int f = 0; f < F; ++f) {
+    if (d->shift_plus[f] < 0) return lt_arg_error("shift_plus must be >= 0");
+    smax = std::max(smax, std::max(d->shift_plus[f], d->shift_minus[f]));
+  }
+  if (d->ldr < d->ldx * smax + d->npw) return lt_arg_error("ldr too small for the shifts named");
+  // K split: enough CTAs to fill every SM a few times over
+  const int tiles = ((P + kChiTile - 1) / kChiTile) * ((Q + kChiTile - 1) / kChiTile) * F;
+  const long long chunks = (long long)d->nbnd * ((d->npw + kChiKc - 1) / kChiKc);
+  int ksplit = std::max(1, (4 * op->num_sms + tiles - 1) / tiles);
+  ksplit = (int)std::min<long long>(ksplit, std::max<long long>(chunks, 1));
+  const size_t nout = (size_t)F * P * Q;
+  sgw_status s;
+  if ((s = op->lt_part.ensure(sizeof(zcd) * ksplit * nout)) != SGW_OK) return s;
+  if ((s = op->lt_sidx.ensure(sizeof(int) * 2 * F)) != SGW_OK) return s;
+  std::vector<int> sidx(2 * F);
+  std::copy(d->shift_plus, d->shift_plus + F, sidx.begin());
+  for (int f = 0; f < F; ++f) sidx[F + f] = d->shift_minus[f] < 0 ? -1 : d->shift_minus[f];
+  ChiArgs a{};
+  a.npert_b = P;
+  a.npert_x = Q;
+  a.nbnd = d->nbnd;
+  a.npw = d->npw;
+  a.nfreq = F;
+  a.ksplit = ksplit;
+  a.weight = d->weight;
+  a.part = op->lt_part.as<zcd>();
+  a.s_plus = op->lt_sidx.as<int>();
+  a.s_minus = op->lt_sidx.as<int>() + F;
+  zcd* chi_out;
+  SGW_CK(cudaEventRecord(op->lev0, op->stream));
+  SGW_CK(cudaMemcpyAsync(op->lt_sidx.p, sidx.data(), sizeof(int) * 2 * F, cudaMemcpyHostToDevice, op->stream));
+  if (d->memory == 0) {
+    const int S = smax + 1;
+    if ((s = op->lt_bb.ensure(sizeof(zcd) * (size_t)P * d->nbnd * d->npw)) != SGW_OK) return s;
+    if ((s = op->lt_xx.ensure(sizeof(zcd) * (size_t)Q * d->nbnd * S * d->npw)) != SGW_OK) return s;
+    if ((s = op->lt_chi.ensure(sizeof(zcd) * (size_t)Q * F * P)) != SGW_OK) return s;
+    SGW_CK(cudaMemcpy2DAsync(op->lt_bb.p, sizeof(zcd) * d->npw, d->bb, sizeof(zcd) * d->ldb, sizeof(zcd) * d->npw,
+                             (size_t)P * d->nbnd, cudaMemcpyHostToDevice, op->stream));
+    for (long long r = 0; r < (long long)Q * d->nbnd; ++r)
+      SGW_CK(cudaMemcpy2DAsync(op->lt_xx.as<zcd>() + (size_t)r * S * d->npw, sizeof(zcd) * d->npw,
+                               reinterpret_cast<const zcd*>(d->xx) + (size_t)r * d->ldr, sizeof(zcd) * d->ldx,
+                               sizeof(zcd) * d->npw, S, cudaMemcpyHostToDevice, op->stream));
+    a.bb = op->lt_bb.as<zcd>();
+    a.ldb = d->npw;
+    a.xx = op->lt_xx.as<zcd>();
+    a.ldx = d->npw;
+    a.ldr = (long long)S * d->npw;
+    chi_out = op->lt_chi.as<zcd>();
+  } else {
+    a.bb = reinterpret_cast<const zcd*>(d->bb);
+    a.ldb = d->ldb;
+    a.xx = reinterpret_cast<const zcd*>(d->xx);
+    a.ldx = d->ldx;
+    a.ldr = d->ldr;
+    chi_out = reinterpret_cast<zcd*>(d->chi);
+  }
+  chi_kernel<<<tiles * ksplit, 256, 0, op->stream>>>(a);
+  SGW_CK(cudaGetLastError());
+  const long long ldc = d->memory == 0 ? P : d->ldc;
+  const int rblocks = (int)std::min<size_t>((nout + 255) / 256, (size_t)op->num_sms * 8);
+  chi_reduce_kernel<<<rblocks, 256, 0, op->stream>>>(a.part, ksplit, F, Q, P, chi_out, ldc);
+  SGW_CK(cudaGetLastError());
+  if (d->memory == 0)
+    SGW_CK(cudaMemcpy2DAsync(d->chi, sizeof(zcd) * d->ldc, chi_out, sizeof(zcd) * P, sizeof(zcd) * P, (size_t)Q * F,
+                             cudaMemcpyDeviceToHost, op->stream));
+  SGW_CK(cudaEventRecord(op->lev1, op->stream));
+  SGW_CK(cudaStreamSynchronize(op->stream));
+  float ms = 0.f;
+  SGW_CK(cudaEventElapsedTime(&ms, op->lev0, op->lev1));
+  op->kernel_ms[K_CHI] = ms;
+  op->kernel_launches[K_CHI] = 2;
+  return SGW_OK;
+}
+
+}  // namespace sgw
+
+extern "C" {
+
+sgw_status sgw_coulomb_rhs(sgw_operator* op, const sgw_rhs_desc* desc) {
+  try {
+    return sgw::coulomb_rhs(op, desc);
+  } catch (...) {
+    sgw::set_error("host exception in sgw_coulomb_rhs");
+    return SGW_ERR_NOMEM;
+  }
+}
+
+sgw_status sgw_chi(sgw_operator* op, const sgw_chi_desc* desc) {
+  try {
+    return sgw::chi(op, desc);
+  } catch (...) {
+    sgw::set_error("host exception in sgw_chi");
+    return SGW_ERR_NOMEM;
+  }
+}
+
+}  // extern "C"

@@ -1,62 +1,49 @@
 """Caller-side glue of the Coulomb (W) and Green's-function solves.
 
-Restates, for the synthetic systems of :mod:`synth`:
-  * the right-hand side  -P_c^+ (Delta V psi_v)  of solve_linter.f90:331-337
-    (dvqpsi_us.f90:96-132 for Delta V psi_v: psi_v scattered on the box with the
-    k map, inverse FFT, times Delta V(r), forward FFT, gathered with the k+q map;
-    then QE orthogonalize for an insulator with S = 1:
-    dvpsi <- -(dvpsi - sum_v evq_v <evq_v|dvpsi>));
-  * the shift list  -(eps_v + omega)  over omega = [w, -w(2:)] or [w, -w]
-    (solve_linter.f90:237-252, 367-369);
-  * the rescaling by wg/wk and the +-omega average (solve_linter.f90:373,
-    462-480);
-  * the Green's-function right-hand sides b = -delta_{G,G'} with shifts -omega
-    (green.f90:195-207).
-The FFTs here use numpy; these functions prepare inputs and post-process
-outputs of the GPU solve, they are not the solve itself.
+  * coulomb_rhs   -P_c^+ (Delta V psi_v) for every band and perturbation on
+                  the GPU (sgw_coulomb_rhs: dvqpsi_us.f90:96-132 and QE
+                  orthogonalize at solve_linter.f90:331-337);
+  * coulomb_shifts  -(eps_v + omega) over omega = [w, -w(2:)] or [w, -w]
+                  (solve_linter.f90:237-252, 367-369);
+  * pm_pairs      which shift holds +omega and which -omega for each
+                  frequency, the input of the fused +-omega average
+                  (solve_linter.f90:462-480);
+  * chi_matrix    the density response on the perturbation set on the GPU
+                  (sgw_chi: the average above, incdrhoscf at :489-497 and the
+                  G' pick of coulomb.f90:146-151);
+  * green_rhs / green_shifts   b = -delta_{G,G'} with shifts -omega
+                  (green.f90:195-207, freqbins.f90:302-323);
+  * coulomb_v / w_from_chi     v = 8 pi / (Omega |q+G|^2) and
+                  W = (1 - v chi)^-1 v (invert_epsilon.f90:23-90).
 """
 from __future__ import annotations
 
+import math
+
 import numpy as np
 
-from . import synth
+from . import solver, synth
 
 
-def _box(system):
-    nr1, nr2, nr3 = [int(v) for v in system["nr"]]
-    return nr1, nr2, nr3
+def dvbare_all(system, perts=None):
+    """Delta V_p(r) for the perturbations `perts` (default: all): (npert, nnr)."""
+    perts = range(len(system["gpert"])) if perts is None else perts
+    return np.stack([synth.dvbare_box(system, ip) for ip in perts])
 
 
-def dvqpsi(system, dvbare_r):
-    """Delta V psi_v on the k+q sphere for every occupied band (dvqpsi_us.f90:96-132).
-
-    dvbare_r: Delta V(r) on the box (flat, index i1 + nr1 (i2 + nr2 i3)).
-    Returns (npw_kq, nocc).
-    """
-    nr1, nr2, nr3 = _box(system)
-    nnr = nr1 * nr2 * nr3
-    evc = system["evc"]
-    out = np.zeros((system["npw"], evc.shape[1]), dtype=np.complex128)
-    for v in range(evc.shape[1]):
-        box = np.zeros(nnr, dtype=np.complex128)
-        box[system["nl_k"]] = evc[:, v]
-        r = np.fft.ifftn(box.reshape(nr3, nr2, nr1)) * nnr  # invfft: exp(+iGr), unscaled
-        r = r.reshape(-1) * dvbare_r
-        g = np.fft.fftn(r.reshape(nr3, nr2, nr1)).reshape(-1) / nnr  # fwfft: exp(-iGr)/N
-        out[:, v] = g[system["nl"]]
-    return out
-
-
-def orthogonalize(system, dvpsi):
-    """-P_c^+ dvpsi = -(dvpsi - evq evq^dagger dvpsi) for an insulator with S = 1."""
-    evq = system["evq"]
-    return -(dvpsi - evq @ (evq.conj().T @ dvpsi))
-
-
-def coulomb_rhs(system, ip):
-    """Right-hand sides of perturbation ip for every occupied band: (nocc, npw)."""
-    dv = synth.dvbare_box(system, ip)
-    return orthogonalize(system, dvqpsi(system, dv)).T.copy()
+def coulomb_rhs(op: solver.PlaneWaveOperator, system, perts=None, device=False):
+    """Right-hand sides of the perturbations `perts` (default: all) for every
+    occupied band, computed on the GPU: (npert * nocc, npw), row p * nocc + v.
+    With device=True the inputs are moved to the GPU first and the result is a
+    CUDA torch tensor."""
+    evc = np.ascontiguousarray(np.asarray(system["evc"]).T)
+    nl_k = np.ascontiguousarray(system["nl_k"], dtype=np.int32)
+    dv = dvbare_all(system, perts)
+    if device:
+        import torch
+        return solver.coulomb_rhs(op, torch.from_numpy(evc).cuda(), torch.from_numpy(nl_k).cuda(),
+                                  torch.from_numpy(dv).cuda())
+    return solver.coulomb_rhs(op, evc, nl_k, dv)
 
 
 def coulomb_shifts(system, freq):
@@ -65,17 +52,31 @@ def coulomb_shifts(system, freq):
     return -(system["et"][:, None] + omega[None, :])
 
 
-def average_pm(dpsi, freq, weight=1.0):
-    """dpsi(:, S) -> dpsi(:, num_freq): rescale by wg/wk and average +-omega (solve_linter.f90:373,462-480)."""
+def pm_pairs(freq):
+    """(shift_plus, shift_minus) per frequency for the omega list of omega_list(freq):
+    +omega at shift f; -omega at nf + f (or nf + f - 1 when freq[0] = 0, whose
+    first frequency has no partner: -1)."""
     freq = np.asarray(freq)
     nf = freq.size
-    d = np.asarray(dpsi) * weight
-    out = d[..., :nf].copy()
+    plus = np.arange(nf, dtype=np.int32)
     if abs(freq[0]) < 1e-14:
-        out[..., 1:] = 0.5 * out[..., 1:] + 0.5 * d[..., nf:]
+        minus = np.concatenate([[-1], nf + np.arange(nf - 1)]).astype(np.int32)
     else:
-        out = 0.5 * out + 0.5 * d[..., nf:]
-    return out
+        minus = (nf + np.arange(nf)).astype(np.int32)
+    return plus, minus
+
+
+def chi_matrix(op, bb, xx, nbnd, freq, weight=1.0):
+    """chi[f, p, q] = -weight * sum_v <b_(p,v) | xbar_(q,v,f)> on the GPU.
+
+    bb: (P * nbnd, n); xx: (Q * nbnd, S, n) (numpy or CUDA torch).
+    Returns (nfreq, P, Q), numpy or torch like the inputs.
+    """
+    plus, minus = pm_pairs(freq)
+    c = solver.chi(op, bb, xx, nbnd, plus, minus, weight)
+    if type(c).__module__.startswith("torch"):
+        return c.permute(1, 2, 0).contiguous()
+    return np.ascontiguousarray(np.transpose(c, (1, 2, 0)))
 
 
 def green_rhs(npw, ig_list):
@@ -93,33 +94,8 @@ def green_shifts(mu, coul_freq):
     return -omega
 
 
-def chi_matrix(bb, x, freq, weight=1.0):
-    """Density response chi[G', G](omega) = -sum_v <b_v^{G'} | x_v^G(omega)>, +-omega averaged.
-
-    The projection of what solve_linter accumulates into drhoscf for each perturbation
-    (incdrhoscf after the +-omega average, solve_linter.f90:462-497) projected on
-    the perturbation set: with b = -P_c Delta V psi_v and Delta psi in the
-    conduction space, <Delta V_{G'} psi_v | Delta psi_v^G> = -<b^{G'} | x^G>.
-    bb: (npert, nocc, n); x: (npert, nocc, S, n).  Works on numpy or torch.
-    Returns (nfreq, npert, npert).
-    """
-    if type(bb).__module__.startswith("torch"):
-        import torch
-        c = -torch.einsum("pvn,qvsn->spq", bb.conj(), x) * weight
-        nf = len(freq)
-        out = c[:nf].clone()
-        if abs(complex(freq[0])) < 1e-14:
-            out[1:] = 0.5 * out[1:] + 0.5 * c[nf:]
-        else:
-            out = 0.5 * out + 0.5 * c[nf:]
-        return out
-    c = -np.einsum("pvn,qvsn->spq", np.conj(bb), x) * weight
-    return np.moveaxis(average_pm(np.moveaxis(c, 0, -1), freq), -1, 0)
-
-
 def coulomb_v(system):
     """Bare Coulomb 8 pi / (Omega |q+G|^2) (Ry) for each perturbation G."""
-    import math
     bmat = {"fcc": np.array([[-1, -1, 1], [1, 1, 1], [-1, 1, -1]]), "sc8": np.eye(3), "sc2": np.eye(3)}[system["lattice"]]
     qg = (system["gpert"] @ bmat + system["qvec"][None, :]) * (2 * math.pi / system["alat"])
     return 8 * math.pi / (system["omega"] * np.sum(qg ** 2, 1))

@@ -243,3 +243,82 @@ def solve_batch(AA: _Operator, bb, sigma, *, lmax=4, threshold=1e-4, max_iter=10
     d.ldb, d.lds, d.ldx, d.ldr = n, S, n, S * n
     _capi.check(_capi.lib().sgw_solve_batch(AA.handle, C.byref(d)), "sgw_solve_batch")
     return xx, ierr, iters
+
+
+def coulomb_rhs(AA: PlaneWaveOperator, evc, nl_k, dvbare, out=None):
+    """b_(p,v) = -P_c^+ (Delta V_p psi_v) on AA's k+q sphere (dvqpsi_us.f90:96-132 + orthogonalize).
+
+    evc: (nocc, npw_k) psi_v at k; nl_k: (npw_k,) int32 box indices; dvbare:
+    (npert, nnr) Delta V_p(r).  numpy arrays go through host memory; CUDA torch
+    tensors (nl_k int32) stay on the device.  Returns bb of shape
+    (npert * nocc, npw), row p * nocc + v.
+    """
+    d = _capi.RhsDesc()
+    if _is_torch(evc):
+        import torch
+        evc = evc.contiguous()
+        dvbare = dvbare.contiguous()
+        nl_k = nl_k.to(torch.int32).contiguous()
+        npert = dvbare.shape[0]
+        nocc = evc.shape[0]
+        bb = out if out is not None else torch.empty((npert * nocc, AA.n), dtype=torch.complex128, device=evc.device)
+        d.memory = 1
+        d.nl_k, d.evc, d.dvbare, d.bb = nl_k.data_ptr(), evc.data_ptr(), dvbare.data_ptr(), bb.data_ptr()
+    else:
+        evc = _c128(evc)
+        dvbare = _c128(np.atleast_2d(dvbare))
+        nl_k = np.ascontiguousarray(nl_k, dtype=np.int32)
+        npert = dvbare.shape[0]
+        nocc = evc.shape[0]
+        bb = out if out is not None else np.zeros((npert * nocc, AA.n), dtype=np.complex128)
+        d.memory = 0
+        d.nl_k, d.evc, d.dvbare, d.bb = nl_k.ctypes.data, evc.ctypes.data, dvbare.ctypes.data, bb.ctypes.data
+    d.npert = npert
+    d.npw_k = evc.shape[1]
+    d.ldk = evc.shape[1]
+    d.lddv = dvbare.shape[1]
+    d.ldb = AA.n
+    _capi.check(_capi.lib().sgw_coulomb_rhs(AA.handle, C.byref(d)), "sgw_coulomb_rhs")
+    return bb
+
+
+def chi(AA: _Operator, bb, xx, nbnd, shift_plus, shift_minus, weight=1.0):
+    """Density response with the +-omega average fused in (solve_linter.f90:462-497, coulomb.f90:146-151).
+
+    bb: (P * nbnd, n) right-hand sides; xx: (Q * nbnd, S, n) solutions;
+    shift_plus / shift_minus: (nfreq,) shift indices of +omega / -omega (-1:
+    none).  Returns chi of shape (Q, nfreq, P) - scrcoul(ig', f, task) order -
+    with chi[q, f, p] = -weight * sum_v <b_(p,v) | xbar_(q,v,f)>.
+    """
+    sp = np.ascontiguousarray(shift_plus, dtype=np.int32)
+    sm = np.ascontiguousarray(shift_minus, dtype=np.int32)
+    nf = sp.size
+    d = _capi.ChiDesc()
+    if _is_torch(bb):
+        import torch
+        bb = bb.contiguous()
+        xx = xx.contiguous()
+        out = torch.empty((xx.shape[0] // nbnd, nf, bb.shape[0] // nbnd), dtype=torch.complex128, device=bb.device)
+        d.memory = 1
+        d.bb, d.xx, d.chi = bb.data_ptr(), xx.data_ptr(), out.data_ptr()
+    else:
+        bb = _c128(bb)
+        xx = _c128(xx)
+        out = np.zeros((xx.shape[0] // nbnd, nf, bb.shape[0] // nbnd), dtype=np.complex128)
+        d.memory = 0
+        d.bb, d.xx, d.chi = bb.ctypes.data, xx.ctypes.data, out.ctypes.data
+    n = bb.shape[1]
+    d.npert_b = bb.shape[0] // nbnd
+    d.npert_x = xx.shape[0] // nbnd
+    d.nbnd = int(nbnd)
+    d.npw = n
+    d.ldb = n
+    d.ldx = n
+    d.ldr = xx.shape[1] * n
+    d.nfreq = nf
+    d.shift_plus = sp.ctypes.data
+    d.shift_minus = sm.ctypes.data
+    d.weight = float(weight)
+    d.ldc = d.npert_b
+    _capi.check(_capi.lib().sgw_chi(AA.handle, C.byref(d)), "sgw_chi")
+    return out

@@ -13,13 +13,14 @@ import numpy as np
 ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
 sys.path.insert(0, ROOT)
 
+from oracle import linter_ref  # noqa: E402
 from oracle import oracle as O  # noqa: E402
 from sternheimergw_gb300 import linter, synth  # noqa: E402
 
 
 def main():
     s, f = synth.config("c0")
-    bb = linter.coulomb_rhs(s, 0)
+    bb = linter_ref.coulomb_rhs(s, 0)
     sh = linter.coulomb_shifts(s, f)
     op = O.PlaneWaveOperator(s)
     xx, ierr, iters, applies = O.bicgstab(op, bb[0], sh[0], lmax=4, threshold=1e-10)

@@ -13,6 +13,7 @@ import numpy as np
 import pytest
 
 import sternheimergw_gb300 as sg
+from oracle import linter_ref
 from oracle import oracle as O
 from sternheimergw_gb300 import linter
 
@@ -136,7 +137,7 @@ def test_pw_apply_green_operator(c0):
 def test_coulomb_solve_c0(c0):
     """Every band of the c0 perturbation (solve_linter.f90:367-374) in one batch."""
     s, f, op, ops = c0
-    bb = linter.coulomb_rhs(s, 0)
+    bb = linter_ref.coulomb_rhs(s, 0)
     sh = linter.coulomb_shifts(s, f)
     x, ierr, iters = sg.solve_batch(op, bb, sh, threshold=1e-10)
     xo, ierro, itero = O.bicgstab_many(ops, bb, sh, threshold=1e-10)
@@ -152,7 +153,7 @@ def test_coulomb_solve_c0(c0):
 def test_history_window_flush(c0):
     """Windows of 1 and 2 outer iterations give the same solution as one window."""
     s, f, op, ops = c0
-    bb = linter.coulomb_rhs(s, 0)
+    bb = linter_ref.coulomb_rhs(s, 0)
     sh = linter.coulomb_shifts(s, f)
     x, _, _ = sg.solve_batch(op, bb, sh, threshold=1e-10)
     for hw in (1, 2):
@@ -181,7 +182,7 @@ def test_green_solve_c0(c0):
 def test_device_pointer_batch(c0):
     import torch
     s, f, op, ops = c0
-    bb = linter.coulomb_rhs(s, 0)
+    bb = linter_ref.coulomb_rhs(s, 0)
     sh = linter.coulomb_shifts(s, f)
     xh, ierrh, _ = sg.solve_batch(op, bb, sh, threshold=1e-10)
     xd, ierrd, itd = sg.solve_batch(op, torch.from_numpy(bb).cuda(), torch.from_numpy(sh).cuda(), threshold=1e-10)
@@ -192,7 +193,7 @@ def test_device_pointer_batch(c0):
 def test_mixed_c0(c0):
     """Mixed precision: FP64 seed residual <= 1e-9 and the response within 1e-6 of FP64."""
     s, f, op, ops = c0
-    bb = linter.coulomb_rhs(s, 0)
+    bb = linter_ref.coulomb_rhs(s, 0)
     sh = linter.coulomb_shifts(s, f)
     x64, ierr64, _ = sg.solve_batch(op, bb, sh, threshold=1e-10)
     xm, ierr, iters = sg.solve_batch(op, bb, sh, threshold=1e-10, precision=1)
@@ -200,8 +201,8 @@ def test_mixed_c0(c0):
     for r in range(bb.shape[0]):
         res = op.apply(sh[r, 0], xm[r, 0]) - bb[r]
         assert np.linalg.norm(res) / np.linalg.norm(bb[r]) <= 1e-9
-    c64 = linter.chi_matrix(bb[None], x64[None], f)
-    cm = linter.chi_matrix(bb[None], xm[None], f)
+    c64 = linter.chi_matrix(op, bb, x64, bb.shape[0], f)
+    cm = linter.chi_matrix(op, bb, xm, bb.shape[0], f)
     assert np.linalg.norm(cm - c64) / np.linalg.norm(c64) < 1e-6
 
 
@@ -211,17 +212,15 @@ def test_mixed_w_error_c4(gpu_lib):
     s, f = synth.config("c4")
     op = sg.PlaneWaveOperator(s)
     npert, nocc = len(s["gpert"]), s["nocc"]
-    B = np.stack([linter.coulomb_rhs(s, ip) for ip in range(npert)])
+    B = np.stack([linter_ref.coulomb_rhs(s, ip) for ip in range(npert)])
     sh1 = linter.coulomb_shifts(s, f)
     bb = B.reshape(npert * nocc, -1)
     sh = np.tile(sh1, (npert, 1))
     x64, e64, _ = sg.solve_batch(op, bb, sh, threshold=1e-10)
     xm, em, _ = sg.solve_batch(op, bb, sh, threshold=1e-10, precision=1)
     assert (e64 == 0).all() and (em == 0).all()
-    X64 = x64.reshape(npert, nocc, sh.shape[1], -1)
-    XM = xm.reshape(npert, nocc, sh.shape[1], -1)
     v = linter.coulomb_v(s)
-    W64 = linter.w_from_chi(linter.chi_matrix(B, X64, f), v)
-    WM = linter.w_from_chi(linter.chi_matrix(B, XM, f), v)
+    W64 = linter.w_from_chi(linter.chi_matrix(op, bb, x64, nocc, f), v)
+    WM = linter.w_from_chi(linter.chi_matrix(op, bb, xm, nocc, f), v)
     err = np.linalg.norm(WM - W64, axis=(1, 2)) / np.linalg.norm(W64, axis=(1, 2))
     assert err.max() < 1e-6, err.max()

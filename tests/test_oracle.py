@@ -128,11 +128,12 @@ def test_pw_apply_matches_dense_h(c0_system):
 
 def test_pw_multishift_matches_direct(c0_system):
     """Plane-wave multishift solve vs dense direct solves on the c0 system."""
+    from oracle import linter_ref
     from sternheimergw_gb300 import linter, synth
     s, f = c0_system
     h = synth.dense_h(s["mill"], s["g2kin"], s["vrs"], s["nr"], s["vkb"], s["dvan"])
     h = h + s["alpha_pv"] * s["evq"] @ s["evq"].conj().T
-    bb = linter.coulomb_rhs(s, 0)
+    bb = linter_ref.coulomb_rhs(s, 0)
     sh = linter.coulomb_shifts(s, f)
     x, ierr, _, _ = O.bicgstab(O.PlaneWaveOperator(s), bb[1], sh[1], lmax=4, threshold=1e-12)
     assert ierr == 0

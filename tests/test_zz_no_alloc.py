@@ -33,10 +33,11 @@ def test_noalloc_matches_batch_twice(c0_system, gpu_lib):
     import torch
 
     import sternheimergw_gb300 as sg
+    from oracle import linter_ref
     from sternheimergw_gb300 import _capi, linter
     s, f = c0_system
     op = sg.PlaneWaveOperator(s)
-    bb = torch.from_numpy(linter.coulomb_rhs(s, 0)).cuda()
+    bb = torch.from_numpy(linter_ref.coulomb_rhs(s, 0)).cuda()
     sh = torch.from_numpy(linter.coulomb_shifts(s, f)).cuda()
     ref, ierr_ref, iters_ref = sg.solve_batch(op, bb, sh, threshold=1e-10)
     assert int(ierr_ref.max()) == 0
