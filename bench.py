@@ -400,7 +400,9 @@ def run_gpu(args, rank, world):
     sg_h = torch.from_numpy(sigma).pin_memory()
     x_h = torch.empty((nrhs, S, n), dtype=torch.complex128).pin_memory()
     e2e_ms = []
-    for k in range(max(1, min(args.steps, 2))):
+    # one untimed call first: it allocates the library's host-path staging buffers
+    sg.solve_batch(op, bb_h.numpy(), sg_h.numpy(), lmax=LMAX, threshold=THRESHOLD, precision=1, out=x_h.numpy())
+    for k in range(max(1, min(args.steps, 3))):
         flush_l2(l2)
         torch.cuda.synchronize()
         t = time.time()

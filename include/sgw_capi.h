@@ -228,6 +228,78 @@ typedef struct sgw_chi_desc {
 
 sgw_status sgw_chi(sgw_operator* op, const sgw_chi_desc* desc);
 
+/* Replace the local potential V_loc(r) of a plane-wave operator (nnr values,
+ * index i1 + nr1 (i2 + nr2 i3), Ry).  Stands for the caller's update of QE's
+ * module array vrs before the solve (h_psi reads it; linear_op.f90:46-144). */
+sgw_status sgw_operator_set_vloc(sgw_operator* op, const double* vrs, int64_t nnr);
+
+/* Adjoint solve for vector-Jacobian products: for every right-hand side r and
+ * shift s, lambda_rs = A(sigma_rs)^-H gbar_rs, i.e. the Hermitian-conjugate
+ * system (H + conj(sigma_rs) + alpha_pv P_v) lambda = gbar, solved by the same
+ * batched BiCGStab(l) machinery with each (r, s) pair as its own single-shift
+ * system (the right-hand side differs per shift).  No counterpart in the
+ * reference, which has no derivatives; the adjoint system is what
+ * select_solver (select_solver.f90:67-161) would solve with shifts conj(sigma).
+ *   sigma[r*lds + s]            the forward shifts
+ *   gbar[r*ldr + s*ldx + g]     cotangent dL/dx (ldr = num_shift * ldx)
+ *   lam[r*ldr + s*ldx + g]      output
+ *   ierr[r*num_shift + s]       per-system reference error code
+ * checkpoint_iters: Krylov iterations (operator applies) after which the
+ * basis is folded into lambda and dropped (0 = 8), so no iterate history is
+ * kept beyond that window.  precision 0 FP64, 1 mixed.  memory 0 host, 1
+ * device. */
+typedef struct sgw_adjoint_desc {
+  int32_t nrhs;
+  int32_t num_shift;
+  int32_t lmax;
+  int32_t max_iter;
+  double threshold;
+  int32_t precision;
+  int32_t memory;
+  int32_t checkpoint_iters;
+  const sgw_zcomplex* sigma;
+  int64_t lds;
+  const sgw_zcomplex* gbar;
+  int64_t ldx;
+  int64_t ldr;
+  sgw_zcomplex* lam;
+  int32_t* ierr;
+} sgw_adjoint_desc;
+
+sgw_status sgw_solve_adjoint(sgw_operator* op, const sgw_adjoint_desc* desc);
+
+/* Vector-Jacobian products of L(x) through the Coulomb solve, given the
+ * forward solutions x and the adjoint solutions lambda (sgw_solve_adjoint):
+ *   grad_vloc[r]   = dL/dV_loc(r) = -(1/N) Re sum_(rhs,s) conj(lambda(r)) x(r)
+ *   grad_dvbare[p*ldg + r] = dL/dRe DeltaV_p(r) + i dL/dIm DeltaV_p(r)
+ *                  = -(1/N) conj( sum_v psi_v(r) conj(mu_pv(r)) ),
+ *                    mu_pv = P_c^+ sum_s lambda_(p nbnd_occ + v, s)
+ * with f(r) the unscaled inverse FFT of a sphere vector (k+q map for x,
+ * lambda, mu; nl_k for psi_v = evc), N = nr1 nr2 nr3.  The right-hand sides
+ * are b_(p,v) = -P_c^+ (Delta V_p psi_v) (sgw_coulomb_rhs); psi_v, eps_v and
+ * P_v are held fixed.  Layout of xx and lam as in sgw_solve_adjoint, rows
+ * r = p*nbnd_occ + v.  Either gradient may be null to skip it; nl_k/evc are
+ * needed for grad_dvbare only.  memory 0 host, 1 device.  No counterpart in
+ * the reference. */
+typedef struct sgw_vjp_desc {
+  int32_t npert;
+  int32_t num_shift;
+  const sgw_zcomplex* xx;
+  const sgw_zcomplex* lam;
+  int64_t ldx;
+  int64_t ldr;
+  int32_t npw_k;
+  const int32_t* nl_k;
+  const sgw_zcomplex* evc;
+  int64_t ldk;
+  double* grad_vloc;
+  sgw_zcomplex* grad_dvbare;
+  int64_t ldg;
+  int32_t memory;
+} sgw_vjp_desc;
+
+sgw_status sgw_vjp(sgw_operator* op, const sgw_vjp_desc* desc);
+
 /* Device time (ms) of the last solve on this handle's stream, measured with
  * CUDA events around the kernels; and the number of kernel launches it used. */
 sgw_status sgw_last_timing(sgw_operator* op, double* ms, int64_t* launches);
@@ -236,7 +308,7 @@ sgw_status sgw_last_timing(sgw_operator* op, double* ms, int64_t* launches);
  * one kernel in the last sgw_solve_batch call: kernel 0 = FP64 multishift
  * solve, 1 = FP32 multishift solve (mixed precision), 2 = FP64 seed residual
  * (mixed precision); kernel 3 = the last sgw_coulomb_rhs (both of its
- * kernels), 4 = the last sgw_chi. */
+ * kernels), 4 = the last sgw_chi, 5 = the last sgw_vjp. */
 sgw_status sgw_kernel_timing(sgw_operator* op, int32_t kernel, double* ms, int64_t* launches);
 
 /* One-line description of the last error on this thread. */

@@ -51,6 +51,20 @@ class ChiDesc(C.Structure):
                 ("weight", C.c_double), ("chi", C.c_void_p), ("ldc", C.c_int64), ("memory", C.c_int32)]
 
 
+class AdjointDesc(C.Structure):
+    _fields_ = [("nrhs", C.c_int32), ("num_shift", C.c_int32), ("lmax", C.c_int32), ("max_iter", C.c_int32),
+                ("threshold", C.c_double), ("precision", C.c_int32), ("memory", C.c_int32),
+                ("checkpoint_iters", C.c_int32), ("sigma", C.c_void_p), ("lds", C.c_int64), ("gbar", C.c_void_p),
+                ("ldx", C.c_int64), ("ldr", C.c_int64), ("lam", C.c_void_p), ("ierr", C.c_void_p)]
+
+
+class VjpDesc(C.Structure):
+    _fields_ = [("npert", C.c_int32), ("num_shift", C.c_int32), ("xx", C.c_void_p), ("lam", C.c_void_p),
+                ("ldx", C.c_int64), ("ldr", C.c_int64), ("npw_k", C.c_int32), ("nl_k", C.c_void_p),
+                ("evc", C.c_void_p), ("ldk", C.c_int64), ("grad_vloc", C.c_void_p), ("grad_dvbare", C.c_void_p),
+                ("ldg", C.c_int64), ("memory", C.c_int32)]
+
+
 # (name, restype, argtypes) of every entry point declared in include/sgw_capi.h
 SIGNATURES = [
     ("sgw_operator_create_pw", C.c_int, [C.POINTER(PwOperatorDesc), C.POINTER(C.c_void_p)]),
@@ -68,6 +82,9 @@ SIGNATURES = [
     ("sgw_solve_batch_noalloc", C.c_int, [C.c_void_p, C.POINTER(BatchDesc)]),
     ("sgw_coulomb_rhs", C.c_int, [C.c_void_p, C.POINTER(RhsDesc)]),
     ("sgw_chi", C.c_int, [C.c_void_p, C.POINTER(ChiDesc)]),
+    ("sgw_operator_set_vloc", C.c_int, [C.c_void_p, C.c_void_p, C.c_int64]),
+    ("sgw_solve_adjoint", C.c_int, [C.c_void_p, C.POINTER(AdjointDesc)]),
+    ("sgw_vjp", C.c_int, [C.c_void_p, C.POINTER(VjpDesc)]),
     ("sgw_last_timing", C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_int64)]),
     ("sgw_kernel_timing", C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_int64)]),
     ("sgw_last_error", C.c_char_p, []),

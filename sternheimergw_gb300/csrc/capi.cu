@@ -383,10 +383,15 @@ static sgw_status solve_batch(sgw_operator* op, const sgw_batch_desc* d) {
     b.iters = op->st_iters.as<int>();
     s = solve_batch_device(op, b, d->precision, d->refine_max, d->refine_threshold);
     if (s != SGW_OK) return s;
-    for (int r = 0; r < R; ++r)
-      SGW_CK(cudaMemcpy2DAsync(reinterpret_cast<zcd*>(d->xx) + (size_t)r * d->ldr, sizeof(zcd) * d->ldx,
-                               op->st_xx.as<zcd>() + (size_t)r * S * n, sizeof(zcd) * n, sizeof(zcd) * n, S,
-                               cudaMemcpyDeviceToHost, op->stream));
+    if (d->ldr == (long long)S * d->ldx) {  // one copy: every (rhs, shift) row at a uniform host pitch
+      SGW_CK(cudaMemcpy2DAsync(d->xx, sizeof(zcd) * d->ldx, op->st_xx.p, sizeof(zcd) * n, sizeof(zcd) * n,
+                               (size_t)R * S, cudaMemcpyDeviceToHost, op->stream));
+    } else {
+      for (int r = 0; r < R; ++r)
+        SGW_CK(cudaMemcpy2DAsync(reinterpret_cast<zcd*>(d->xx) + (size_t)r * d->ldr, sizeof(zcd) * d->ldx,
+                                 op->st_xx.as<zcd>() + (size_t)r * S * n, sizeof(zcd) * n, sizeof(zcd) * n, S,
+                                 cudaMemcpyDeviceToHost, op->stream));
+    }
     SGW_CK(cudaMemcpyAsync(d->ierr, op->st_ierr.p, sizeof(int) * R, cudaMemcpyDeviceToHost, op->stream));
     if (d->iters) SGW_CK(cudaMemcpyAsync(d->iters, op->st_iters.p, sizeof(int) * R, cudaMemcpyDeviceToHost, op->stream));
     SGW_CK(cudaEventRecord(op->ev1, op->stream));

@@ -85,7 +85,7 @@ struct Workspace {
 };
 
 // Kernel kinds timed with CUDA events on the operator's stream.
-enum KernelKind { K_MSBICG_F64 = 0, K_MSBICG_F32 = 1, K_RESIDUAL_F64 = 2, K_RHS = 3, K_CHI = 4, K_NUM = 5 };
+enum KernelKind { K_MSBICG_F64 = 0, K_MSBICG_F32 = 1, K_RESIDUAL_F64 = 2, K_RHS = 3, K_CHI = 4, K_VJP = 5, K_NUM = 6 };
 constexpr int kMaxTimedLaunches = 64;
 
 }  // namespace sgw

@@ -8,6 +8,7 @@
 #include "chi.cuh"
 #include "host.cuh"
 #include "rhs.cuh"
+#include "vjp.cuh"
 
 namespace sgw {
 
@@ -184,9 +185,270 @@ static sgw_status chi(sgw_operator* op, const sgw_chi_desc* d) {
   return SGW_OK;
 }
 
+// lambda_rs = A(sigma_rs)^-H g_rs = (H + conj(sigma_rs) + alpha_pv P_v)^-1 g_rs: every (rhs, shift)
+// pair is its own single-shift system of the batched solver.
+__global__ void adjoint_pack_kernel(const zcd* sigma, long long lds, int nrhs, int nshift, zcd* out) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nrhs * nshift; i += gridDim.x * blockDim.x) {
+    const int r = i / nshift, s = i - r * nshift;
+    out[i] = conj(sigma[(size_t)r * lds + s]);
+  }
+}
+
+static sgw_status solve_adjoint(sgw_operator* op, const sgw_adjoint_desc* d) {
+  if (!op || !d) return lt_arg_error("null argument");
+  const int R = d->nrhs, S = d->num_shift, n = op->n;
+  if (R < 0 || S < 1 || d->lmax < 1 || d->lmax > kMaxL - 1 || d->max_iter < 1 || d->memory < 0 || d->memory > 1 ||
+      d->precision < 0 || d->precision > 1)
+    return lt_arg_error("invalid adjoint description");
+  if (R == 0) return SGW_OK;
+  if (!d->sigma || !d->gbar || !d->lam || !d->ierr) return lt_arg_error("null adjoint array");
+  if (d->lds < S || d->ldx < n || d->ldr != (long long)S * d->ldx)
+    return lt_arg_error("adjoint layout must be packed per right-hand side: ldr = num_shift * ldx, ldx >= n");
+  const long long M = (long long)R * S;
+  if (M > 0x7fffffffLL) return lt_arg_error("too many adjoint systems");
+  const int ck = d->checkpoint_iters > 0 ? d->checkpoint_iters : 8;
+  BatchDev b{(int)M, 1, d->lmax, d->max_iter, std::max(1, (ck + 2 * d->lmax - 1) / (2 * d->lmax)), d->threshold,
+             nullptr, d->ldx, nullptr, 1, nullptr, d->ldx, d->ldx, nullptr, nullptr};
+  sgw_status s;
+  if ((s = op->lt_sidx.ensure(sizeof(zcd) * M)) != SGW_OK) return s;
+  if ((s = op->st_iters.ensure(sizeof(int) * M)) != SGW_OK) return s;
+  zcd* sig = op->lt_sidx.as<zcd>();
+  op->last_launches = 0;
+  op->kev_used = 0;
+  if (d->memory == 1) {
+    SGW_CK(cudaEventRecord(op->ev0, op->stream));
+    adjoint_pack_kernel<<<std::max(1, std::min<int>((int)((M + 255) / 256), op->num_sms * 4)), 256, 0, op->stream>>>(
+        reinterpret_cast<const zcd*>(d->sigma), d->lds, R, S, sig);
+    SGW_CK(cudaGetLastError());
+    b.bb = d->gbar;
+    b.xx = d->lam;
+    b.ierr = d->ierr;
+  } else {
+    std::vector<zcd> sh(M);
+    for (int r = 0; r < R; ++r)
+      for (int k = 0; k < S; ++k) {
+        const sgw_zcomplex z = d->sigma[(size_t)r * d->lds + k];
+        sh[(size_t)r * S + k] = zcd{z.re, -z.im};
+      }
+    if ((s = op->st_bb.ensure(sizeof(zcd) * M * n)) != SGW_OK) return s;
+    if ((s = op->st_xx.ensure(sizeof(zcd) * M * n)) != SGW_OK) return s;
+    if ((s = op->st_ierr.ensure(sizeof(int) * M)) != SGW_OK) return s;
+    SGW_CK(cudaEventRecord(op->ev0, op->stream));
+    SGW_CK(cudaMemcpyAsync(sig, sh.data(), sizeof(zcd) * M, cudaMemcpyHostToDevice, op->stream));
+    SGW_CK(cudaMemcpy2DAsync(op->st_bb.p, sizeof(zcd) * n, d->gbar, sizeof(zcd) * d->ldx, sizeof(zcd) * n, M,
+                             cudaMemcpyHostToDevice, op->stream));
+    b.bb = op->st_bb.p;
+    b.ldb = n;
+    b.xx = op->st_xx.p;
+    b.ldx = n;
+    b.ldr = n;
+    b.ierr = op->st_ierr.as<int>();
+  }
+  b.sigma = sig;
+  b.iters = op->st_iters.as<int>();
+  s = d->precision == 0 ? run_msbicg<double>(op, b) : solve_mixed(op, b, 0, 0.0);
+  if (s != SGW_OK) return s;
+  if (d->memory == 0) {
+    SGW_CK(cudaMemcpy2DAsync(d->lam, sizeof(zcd) * d->ldx, op->st_xx.p, sizeof(zcd) * n, sizeof(zcd) * n, M,
+                             cudaMemcpyDeviceToHost, op->stream));
+    SGW_CK(cudaMemcpyAsync(d->ierr, op->st_ierr.p, sizeof(int) * M, cudaMemcpyDeviceToHost, op->stream));
+  }
+  SGW_CK(cudaEventRecord(op->ev1, op->stream));
+  SGW_CK(cudaStreamSynchronize(op->stream));
+  float ms = 0.f;
+  SGW_CK(cudaEventElapsedTime(&ms, op->ev0, op->ev1));
+  op->last_ms = ms;
+  return SGW_OK;
+}
+
+static sgw_status vjp(sgw_operator* op, const sgw_vjp_desc* d) {
+  if (!op || !d) return lt_arg_error("null argument");
+  if (op->kind != 1) return lt_arg_error("sgw_vjp needs a plane-wave operator");
+  const PwView<double>& v = op->pw64;
+  const int nocc = v.nocc, npw = v.npw, P = d->npert, S = d->num_shift;
+  const int nnr = v.nnr;
+  if (P < 0 || S < 1 || d->npw_k < 0 || d->memory < 0 || d->memory > 1) return lt_arg_error("invalid vjp description");
+  if (P == 0 || nocc == 0) return SGW_OK;
+  if (!d->xx || !d->lam || (!d->grad_vloc && !d->grad_dvbare)) return lt_arg_error("null vjp array");
+  if (d->grad_dvbare && (!d->nl_k || !d->evc || d->ldk < d->npw_k || d->ldg < nnr))
+    return lt_arg_error("the Delta V gradient needs nl_k, evc (ldk >= npw_k) and ldg >= nnr");
+  if (d->ldx < npw || d->ldr < d->ldx * (S - 1) + npw) return lt_arg_error("leading dimensions too small");
+  const long long R = (long long)P * nocc;
+  const int nslot_v = (int)std::min<long long>(R * S, op->num_sms);
+  const int nslot_p = std::min(P, op->num_sms);
+  const int nslot = std::max(nslot_v, nslot_p);
+  sgw_status s;
+  if ((s = op->lt_box.ensure(sizeof(zcd) * 2 * (size_t)nslot * nnr)) != SGW_OK) return s;
+  if ((s = op->lt_part.ensure(sizeof(double) * (size_t)nslot_v * nnr)) != SGW_OK) return s;
+  if ((s = op->lt_chi.ensure(sizeof(zcd) * (size_t)nslot_p * v.npwx)) != SGW_OK) return s;
+  if ((s = op->lt_psi.ensure(sizeof(zcd) * (size_t)nocc * nnr)) != SGW_OK) return s;
+  if ((s = op->lt_flag.ensure(sizeof(int))) != SGW_OK) return s;
+  VjpArgs a{};
+  a.nr1 = v.nr1;
+  a.nr2 = v.nr2;
+  a.nr3 = v.nr3;
+  a.p1 = v.p1;
+  a.p2 = v.p2;
+  a.p3 = v.p3;
+  a.tw = v.tw;
+  a.npw = npw;
+  a.npwx = v.npwx;
+  a.nocc = nocc;
+  a.npert = P;
+  a.nshift = S;
+  a.nl = op->nlkq.as<int>();
+  a.evq = v.evq;
+  a.psi_r = op->lt_psi.as<zcd>();
+  a.box = op->lt_box.as<zcd>();
+  a.sphere = op->lt_chi.as<zcd>();
+  a.part_v = op->lt_part.as<double>();
+  a.ldg = nnr;
+  RhsArgs ra{};
+  ra.nocc = nocc;
+  ra.npw_k = d->npw_k;
+  ra.nr1 = v.nr1;
+  ra.nr2 = v.nr2;
+  ra.nr3 = v.nr3;
+  ra.p1 = v.p1;
+  ra.p2 = v.p2;
+  ra.p3 = v.p3;
+  ra.tw = v.tw;
+  ra.psi_r = op->lt_psi.as<zcd>();
+  ra.bad_index = op->lt_flag.as<int>();
+  double* gv = nullptr;
+  zcd* gd = nullptr;
+  SGW_CK(cudaMemsetAsync(ra.bad_index, 0, sizeof(int), op->stream));
+  SGW_CK(cudaEventRecord(op->lev0, op->stream));
+  if (d->memory == 0) {
+    if (d->grad_dvbare)
+      for (int g = 0; g < d->npw_k; ++g)
+        if (d->nl_k[g] < 0 || d->nl_k[g] >= nnr) return lt_arg_error("nl_k index outside the FFT box");
+    const size_t M = (size_t)R * S;
+    if ((s = op->st_xx.ensure(sizeof(zcd) * M * npw)) != SGW_OK) return s;
+    if ((s = op->st_bb.ensure(sizeof(zcd) * M * npw)) != SGW_OK) return s;
+    for (long long r = 0; r < R; ++r) {
+      SGW_CK(cudaMemcpy2DAsync(op->st_xx.as<zcd>() + (size_t)r * S * npw, sizeof(zcd) * npw,
+                               reinterpret_cast<const zcd*>(d->xx) + (size_t)r * d->ldr, sizeof(zcd) * d->ldx,
+                               sizeof(zcd) * npw, S, cudaMemcpyHostToDevice, op->stream));
+      SGW_CK(cudaMemcpy2DAsync(op->st_bb.as<zcd>() + (size_t)r * S * npw, sizeof(zcd) * npw,
+                               reinterpret_cast<const zcd*>(d->lam) + (size_t)r * d->ldr, sizeof(zcd) * d->ldx,
+                               sizeof(zcd) * npw, S, cudaMemcpyHostToDevice, op->stream));
+    }
+    a.xx = op->st_xx.as<zcd>();
+    a.lam = op->st_bb.as<zcd>();
+    a.ldx = npw;
+    a.ldr = (long long)S * npw;
+    if (d->grad_dvbare) {
+      if ((s = op->lt_nlk.ensure(sizeof(int) * std::max(d->npw_k, 1))) != SGW_OK) return s;
+      if ((s = op->lt_evc.ensure(sizeof(zcd) * (size_t)nocc * std::max(d->npw_k, 1))) != SGW_OK) return s;
+      SGW_CK(cudaMemcpyAsync(op->lt_nlk.p, d->nl_k, sizeof(int) * d->npw_k, cudaMemcpyHostToDevice, op->stream));
+      SGW_CK(cudaMemcpy2DAsync(op->lt_evc.p, sizeof(zcd) * d->npw_k, d->evc, sizeof(zcd) * d->ldk,
+                               sizeof(zcd) * d->npw_k, nocc, cudaMemcpyHostToDevice, op->stream));
+      ra.nl_k = op->lt_nlk.as<int>();
+      ra.evc = op->lt_evc.as<zcd>();
+      ra.ldk = d->npw_k;
+    }
+    if ((s = op->lt_dv.ensure(sizeof(zcd) * ((size_t)P * nnr + nnr))) != SGW_OK) return s;
+    gd = op->lt_dv.as<zcd>();
+    gv = reinterpret_cast<double*>(gd + (size_t)P * nnr);
+  } else {
+    a.xx = reinterpret_cast<const zcd*>(d->xx);
+    a.lam = reinterpret_cast<const zcd*>(d->lam);
+    a.ldx = d->ldx;
+    a.ldr = d->ldr;
+    ra.nl_k = d->nl_k;
+    ra.evc = reinterpret_cast<const zcd*>(d->evc);
+    ra.ldk = d->ldk;
+    gd = reinterpret_cast<zcd*>(d->grad_dvbare);
+    gv = d->grad_vloc;
+    a.ldg = d->ldg;
+  }
+  const size_t tw_bytes = sizeof(zcd) * (v.nr1 + v.nr2 + v.nr3);
+  int launches = 0;
+  if (d->grad_vloc) {
+    vjp_vloc_kernel<<<nslot_v, 256, tw_bytes, op->stream>>>(a);
+    SGW_CK(cudaGetLastError());
+    vjp_vloc_reduce<<<std::max(1, std::min((nnr + 255) / 256, op->num_sms * 4)), 256, 0, op->stream>>>(
+        a.part_v, nslot_v, nnr, gv);
+    SGW_CK(cudaGetLastError());
+    launches += 2;
+  }
+  if (d->grad_dvbare) {
+    rhs_psi_kernel<<<nocc, 256, tw_bytes, op->stream>>>(ra);
+    SGW_CK(cudaGetLastError());
+    a.grad_dv = gd;
+    vjp_dv_kernel<<<nslot_p, 256, tw_bytes + sizeof(zcd) * nocc, op->stream>>>(a);
+    SGW_CK(cudaGetLastError());
+    launches += 2;
+  }
+  if (d->memory == 0) {
+    if (d->grad_vloc)
+      SGW_CK(cudaMemcpyAsync(d->grad_vloc, gv, sizeof(double) * nnr, cudaMemcpyDeviceToHost, op->stream));
+    if (d->grad_dvbare)
+      SGW_CK(cudaMemcpy2DAsync(d->grad_dvbare, sizeof(zcd) * d->ldg, gd, sizeof(zcd) * nnr, sizeof(zcd) * nnr, P,
+                               cudaMemcpyDeviceToHost, op->stream));
+  }
+  SGW_CK(cudaEventRecord(op->lev1, op->stream));
+  int bad = 0;
+  SGW_CK(cudaMemcpyAsync(&bad, ra.bad_index, sizeof(int), cudaMemcpyDeviceToHost, op->stream));
+  SGW_CK(cudaStreamSynchronize(op->stream));
+  float ms = 0.f;
+  SGW_CK(cudaEventElapsedTime(&ms, op->lev0, op->lev1));
+  op->kernel_ms[K_VJP] = ms;
+  op->kernel_launches[K_VJP] = launches;
+  if (bad) return lt_arg_error("nl_k index outside the FFT box");
+  return SGW_OK;
+}
+
+template <typename T>
+static sgw_status upload_vloc(sgw_operator* op, const double* vrs, long long nnr, DevBuf& dst) {
+  std::vector<T> h(nnr);
+  for (long long i = 0; i < nnr; ++i) h[i] = (T)vrs[i];
+  SGW_CK(cudaStreamSynchronize(op->stream));
+  SGW_CK(cudaMemcpy(dst.p, h.data(), sizeof(T) * nnr, cudaMemcpyHostToDevice));
+  return SGW_OK;
+}
+
+static sgw_status set_vloc(sgw_operator* op, const double* vrs, long long nnr) {
+  if (!op || !vrs) return lt_arg_error("null argument");
+  if (op->kind != 1) return lt_arg_error("sgw_operator_set_vloc needs a plane-wave operator");
+  if (nnr != op->pw64.nnr) return lt_arg_error("V_loc size differs from the FFT box");
+  sgw_status s = upload_vloc<double>(op, vrs, nnr, op->vrs64);
+  if (s == SGW_OK) s = upload_vloc<float>(op, vrs, nnr, op->vrs32);
+  return s;
+}
+
 }  // namespace sgw
 
 extern "C" {
+
+sgw_status sgw_solve_adjoint(sgw_operator* op, const sgw_adjoint_desc* desc) {
+  try {
+    return sgw::solve_adjoint(op, desc);
+  } catch (...) {
+    sgw::set_error("host exception in sgw_solve_adjoint");
+    return SGW_ERR_NOMEM;
+  }
+}
+
+sgw_status sgw_vjp(sgw_operator* op, const sgw_vjp_desc* desc) {
+  try {
+    return sgw::vjp(op, desc);
+  } catch (...) {
+    sgw::set_error("host exception in sgw_vjp");
+    return SGW_ERR_NOMEM;
+  }
+}
+
+sgw_status sgw_operator_set_vloc(sgw_operator* op, const double* vrs, int64_t nnr) {
+  try {
+    return sgw::set_vloc(op, vrs, nnr);
+  } catch (...) {
+    sgw::set_error("host exception in sgw_operator_set_vloc");
+    return SGW_ERR_NOMEM;
+  }
+}
+
 
 sgw_status sgw_coulomb_rhs(sgw_operator* op, const sgw_rhs_desc* desc) {
   try {

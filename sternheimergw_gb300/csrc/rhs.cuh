@@ -19,6 +19,12 @@
 
 namespace sgw {
 
+// FFT box geometry: nr1 x nr2 x nr3, index i1 + nr1 (i2 + nr2 i3), plans per axis.
+struct BoxGeom {
+  int nr1, nr2, nr3;
+  FftPlan p1, p2, p3;
+};
+
 struct RhsArgs {
   int npert, nocc, npw_k, npw, npwx, nr1, nr2, nr3;
   const int* nl_k;    // [npw_k] box index of each k-sphere point
@@ -75,15 +81,17 @@ __device__ void box_axis(zcd* box, int n1, int n2, int n3, const FftPlan& p, con
   __syncthreads();
 }
 
-template <int S>
-__device__ void box_fft3d(zcd* box, const RhsArgs& a, const zcd* tw) {
+// Unscaled 3-D transform of a whole box; tw = the three axes' tables back to back.
+template <int S, class G>
+__device__ void box_fft3d(zcd* box, const G& a, const zcd* tw) {
   box_axis<S, 0>(box, a.nr1, a.nr2, a.nr3, a.p1, tw);
   box_axis<S, 1>(box, a.nr1, a.nr2, a.nr3, a.p2, tw + a.nr1);
   box_axis<S, 2>(box, a.nr1, a.nr2, a.nr3, a.p3, tw + a.nr1 + a.nr2);
 }
 
-__device__ inline void load_twiddles(const RhsArgs& a, zcd* sm) {
-  for (int e = threadIdx.x; e < a.nr1 + a.nr2 + a.nr3; e += blockDim.x) sm[e] = a.tw[e];
+template <class G>
+__device__ inline void load_twiddles(const G& a, const zcd* tw, zcd* sm) {
+  for (int e = threadIdx.x; e < a.nr1 + a.nr2 + a.nr3; e += blockDim.x) sm[e] = tw[e];
   __syncthreads();
 }
 
@@ -91,7 +99,7 @@ __device__ inline void load_twiddles(const RhsArgs& a, zcd* sm) {
 __global__ void __launch_bounds__(256, 1) rhs_psi_kernel(RhsArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   zcd* tw = reinterpret_cast<zcd*>(smem_raw);
-  load_twiddles(a, tw);
+  load_twiddles(a, a.tw, tw);
   const int nnr = a.nr1 * a.nr2 * a.nr3;
   for (int v = blockIdx.x; v < a.nocc; v += gridDim.x) {
     zcd* box = a.psi_r + (size_t)v * nnr;
@@ -114,7 +122,7 @@ __global__ void __launch_bounds__(256, 1) rhs_kernel(RhsArgs a) {
   __shared__ zcd red[32];
   zcd* tw = reinterpret_cast<zcd*>(smem_raw);
   zcd* proj = tw + a.nr1 + a.nr2 + a.nr3;  // [nocc]
-  load_twiddles(a, tw);
+  load_twiddles(a, a.tw, tw);
   const int tid = threadIdx.x, nt = blockDim.x;
   const int nnr = a.nr1 * a.nr2 * a.nr3;
   const double scale = 1.0 / (double)nnr;  // fwfft carries 1/N

@@ -159,6 +159,13 @@ class PlaneWaveOperator(_Operator):
         h = C.c_void_p()
         _capi.check(_capi.lib().sgw_operator_create_pw(C.byref(d), C.byref(h)), "sgw_operator_create_pw")
         self.handle = h
+        self.nnr = int(np.prod([int(v) for v in s["nr"]]))
+        self.nocc = int(k["evq"].shape[1])
+
+    def set_vloc(self, vrs):
+        """Replace V_loc(r) (nnr reals, Ry) on the device (the caller's vrs update before h_psi)."""
+        v = np.ascontiguousarray(vrs, dtype=np.float64).reshape(-1)
+        _capi.check(_capi.lib().sgw_operator_set_vloc(self.handle, v.ctypes.data, v.size), "sgw_operator_set_vloc")
 
 
 def bicgstab(config: BicgstabConfig, AA: _Operator, bb, sigma):
@@ -322,3 +329,93 @@ def chi(AA: _Operator, bb, xx, nbnd, shift_plus, shift_minus, weight=1.0):
     d.ldc = d.npert_b
     _capi.check(_capi.lib().sgw_chi(AA.handle, C.byref(d)), "sgw_chi")
     return out
+
+
+def solve_adjoint(AA: _Operator, gbar, sigma, *, lmax=4, threshold=1e-10, max_iter=10000, precision=0,
+                  checkpoint_iters=8):
+    """lambda_rs = A(sigma_rs)^-H gbar_rs: the Hermitian-conjugate systems at conj(sigma), one
+    single-shift system per (rhs, shift) pair.  gbar: (nrhs, S, n); sigma: (nrhs, S).
+    numpy (host) or CUDA torch (device).  Returns (lam[nrhs, S, n], ierr[nrhs, S])."""
+    d = _capi.AdjointDesc()
+    if _is_torch(gbar):
+        import torch
+        gbar = gbar.contiguous()
+        sigma = sigma.contiguous()
+        R, S, n = gbar.shape
+        lam = torch.empty_like(gbar)
+        ierr = torch.zeros((R, S), dtype=torch.int32, device=gbar.device)
+        d.memory = 1
+        d.sigma, d.gbar, d.lam, d.ierr = sigma.data_ptr(), gbar.data_ptr(), lam.data_ptr(), ierr.data_ptr()
+    else:
+        gbar = _c128(gbar)
+        sigma = _c128(sigma)
+        R, S, n = gbar.shape
+        lam = np.zeros_like(gbar)
+        ierr = np.zeros((R, S), dtype=np.int32)
+        d.memory = 0
+        d.sigma, d.gbar, d.lam, d.ierr = sigma.ctypes.data, gbar.ctypes.data, lam.ctypes.data, ierr.ctypes.data
+    if n != AA.n or sigma.shape[0] != R or sigma.shape[1] != S:
+        raise ValueError("adjoint shapes do not match the operator / shifts")
+    d.nrhs, d.num_shift, d.lmax, d.max_iter = R, S, int(lmax), int(max_iter)
+    d.threshold = float(threshold)
+    d.precision = int(precision)
+    d.checkpoint_iters = int(checkpoint_iters)
+    d.lds, d.ldx, d.ldr = S, n, S * n
+    _capi.check(_capi.lib().sgw_solve_adjoint(AA.handle, C.byref(d)), "sgw_solve_adjoint")
+    return lam, ierr
+
+
+def vjp(AA: PlaneWaveOperator, xx, lam, *, evc=None, nl_k=None, want_vloc=True, want_dvbare=True):
+    """Gradients of a real loss through the Coulomb solve from the forward solutions xx and the
+    adjoint solutions lam (both (npert * nocc, S, n), rows p * nocc + v):
+    grad_vloc (nnr,) real and grad_dvbare (npert, nnr) complex (dL/dRe + i dL/dIm).
+    evc (nocc, npw_k) and nl_k are needed for grad_dvbare.  numpy or CUDA torch."""
+    d = _capi.VjpDesc()
+    R, S, n = xx.shape
+    if _is_torch(xx):
+        import torch
+        xx = xx.contiguous()
+        lam = lam.contiguous()
+        dev = xx.device
+        gv = torch.empty(AA.nnr, dtype=torch.float64, device=dev) if want_vloc else None
+        d.memory = 1
+        d.xx, d.lam = xx.data_ptr(), lam.data_ptr()
+        if want_dvbare:
+            evc = evc.contiguous()
+            nl_k = nl_k.to(torch.int32).contiguous()
+            nocc = evc.shape[0]
+            gd = torch.empty((R // nocc, AA.nnr), dtype=torch.complex128, device=dev)
+            d.nl_k, d.evc, d.grad_dvbare = nl_k.data_ptr(), evc.data_ptr(), gd.data_ptr()
+        else:
+            gd = None
+        if gv is not None:
+            d.grad_vloc = gv.data_ptr()
+    else:
+        xx = _c128(xx)
+        lam = _c128(lam)
+        gv = np.zeros(AA.nnr, dtype=np.float64) if want_vloc else None
+        d.memory = 0
+        d.xx, d.lam = xx.ctypes.data, lam.ctypes.data
+        if want_dvbare:
+            evc = _c128(evc)
+            nl_k = np.ascontiguousarray(nl_k, dtype=np.int32)
+            nocc = evc.shape[0]
+            gd = np.zeros((R // nocc, AA.nnr), dtype=np.complex128)
+            d.nl_k, d.evc, d.grad_dvbare = nl_k.ctypes.data, evc.ctypes.data, gd.ctypes.data
+        else:
+            gd = None
+        if gv is not None:
+            d.grad_vloc = gv.ctypes.data
+    if want_dvbare:
+        d.npw_k = evc.shape[1]
+        d.ldk = evc.shape[1]
+        d.ldg = AA.nnr
+        if R % nocc:
+            raise ValueError("rows of xx must be npert * nocc")
+        d.npert = R // nocc
+    else:
+        d.npert = R // int(AA.nocc)
+    d.num_shift = S
+    d.ldx, d.ldr = n, S * n
+    _capi.check(_capi.lib().sgw_vjp(AA.handle, C.byref(d)), "sgw_vjp")
+    return gv, gd
