@@ -300,6 +300,56 @@ typedef struct sgw_vjp_desc {
 
 sgw_status sgw_vjp(sgw_operator* op, const sgw_vjp_desc* desc);
 
+/* Uneven batches: many independent systems - each its own plane-wave
+ * operator (G-sphere, FFT box, bands), right-hand sides and shift list -
+ * solved together.  Every iteration stage is one persistent launch over the
+ * (system, rhs) items of all systems, longest first, with converged systems
+ * dropping out in place (per FFT variant present: register-line or
+ * shared-memory FFT).  No counterpart in the reference, which solves one
+ * right-hand side per select_solver call (solve_linter.f90:367-374).
+ * descs[i] follows sgw_solve_batch with device pointers (memory = 1) and a
+ * non-null iters.  The plan owns the scratch memory; with use_graph = 1 the
+ * whole solve is captured once as a CUDA graph at creation and each run
+ * replays it (the pointers in descs must stay valid).  Runs of different
+ * plans are serialised inside the library (one constant-memory table). */
+typedef struct sgw_multi_options {
+  int32_t precision;        /* 0 FP64, 1 mixed (as sgw_solve_batch) */
+  int32_t refine_max;       /* mixed: FP64 refinement rounds, all launched (0 = 4) */
+  double refine_threshold;  /* mixed: relative FP64 seed residual target (0 = 1e-9) */
+  int32_t use_graph;
+} sgw_multi_options;
+
+typedef struct sgw_multi sgw_multi;
+
+sgw_status sgw_multi_create(int32_t nsys, sgw_operator* const* ops, const sgw_batch_desc* descs,
+                            const sgw_multi_options* opt, sgw_multi** plan);
+
+/* Run the plan; total_ms = CUDA-event time of the whole solve, sys_ms[i] =
+ * completion time of system i from the start of the run (optional). */
+sgw_status sgw_multi_run(sgw_multi* plan, double* total_ms, double* sys_ms);
+
+/* Kernel launches per run, launch groups per stage, whether a graph is used. */
+sgw_status sgw_multi_info(sgw_multi* plan, int64_t* launches_per_run, int32_t* stage_launch_groups, int32_t* graph);
+
+sgw_status sgw_multi_destroy(sgw_multi* plan);
+
+/* Autotuner: time the operator's apply kernel under every FFT launch shape
+ * that fits (register-line or shared-memory FFT, planes in flight, column
+ * store in shared or global memory) and keep the fastest for the FP64
+ * (precision 0) or FP32 (precision 1) kernels.  Results are cached per
+ * geometry for the process (cached = 1: no timing was needed).  No
+ * counterpart in the reference. */
+typedef struct sgw_tune_result {
+  int32_t lines;
+  int32_t col_in_smem;
+  int32_t planes;
+  double us_per_apply;
+  int32_t candidates;
+  int32_t cached;
+} sgw_tune_result;
+
+sgw_status sgw_operator_autotune(sgw_operator* op, int32_t precision, sgw_tune_result* result);
+
 /* Device time (ms) of the last solve on this handle's stream, measured with
  * CUDA events around the kernels; and the number of kernel launches it used. */
 sgw_status sgw_last_timing(sgw_operator* op, double* ms, int64_t* launches);

@@ -65,6 +65,16 @@ class VjpDesc(C.Structure):
                 ("ldg", C.c_int64), ("memory", C.c_int32)]
 
 
+class MultiOptions(C.Structure):
+    _fields_ = [("precision", C.c_int32), ("refine_max", C.c_int32), ("refine_threshold", C.c_double),
+                ("use_graph", C.c_int32)]
+
+
+class TuneResult(C.Structure):
+    _fields_ = [("lines", C.c_int32), ("col_in_smem", C.c_int32), ("planes", C.c_int32),
+                ("us_per_apply", C.c_double), ("candidates", C.c_int32), ("cached", C.c_int32)]
+
+
 # (name, restype, argtypes) of every entry point declared in include/sgw_capi.h
 SIGNATURES = [
     ("sgw_operator_create_pw", C.c_int, [C.POINTER(PwOperatorDesc), C.POINTER(C.c_void_p)]),
@@ -85,6 +95,12 @@ SIGNATURES = [
     ("sgw_operator_set_vloc", C.c_int, [C.c_void_p, C.c_void_p, C.c_int64]),
     ("sgw_solve_adjoint", C.c_int, [C.c_void_p, C.POINTER(AdjointDesc)]),
     ("sgw_vjp", C.c_int, [C.c_void_p, C.POINTER(VjpDesc)]),
+    ("sgw_multi_create", C.c_int, [C.c_int32, C.POINTER(C.c_void_p), C.POINTER(BatchDesc), C.POINTER(MultiOptions),
+                                   C.POINTER(C.c_void_p)]),
+    ("sgw_multi_run", C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.c_void_p]),
+    ("sgw_multi_info", C.c_int, [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
+    ("sgw_multi_destroy", C.c_int, [C.c_void_p]),
+    ("sgw_operator_autotune", C.c_int, [C.c_void_p, C.c_int32, C.POINTER(TuneResult)]),
     ("sgw_last_timing", C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_int64)]),
     ("sgw_kernel_timing", C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_int64)]),
     ("sgw_last_error", C.c_char_p, []),

@@ -72,7 +72,7 @@ sgw_status run_msbicg(sgw_operator* op, const BatchDev& b) {
   a.iters = b.iters;
   a.counter = ws.counter.as<int>();
   a.ws_vec = ws.vec.as<cplx<T>>();
-  a.nvec_slot = nvec_slot;
+  a.vec_stride = nvec_slot * npwx;
   a.ws_coef = ws.coef.as<zcd>();
   a.ncoef_slot = L.total;
   a.Kcap = Kcap;
@@ -189,7 +189,7 @@ sgw_status run_msbicg_in(sgw_operator* op, const BatchDev& b, unsigned char* reg
     a.ldx = b.ldx;
     a.ldr = b.ldr;
     a.ierr = b.ierr;
-    a.nvec_slot = (long long)(vec_b / (sizeof(cplx<T>) * npwx));
+    a.vec_stride = (long long)(vec_b / sizeof(cplx<T>));
     a.ncoef_slot = (long long)(coef_b / sizeof(zcd));
     a.Kcap = Kcap;
     a.P = P;

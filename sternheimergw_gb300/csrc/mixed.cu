@@ -18,121 +18,10 @@
 
 #include "host.cuh"
 #include "launch.cuh"
+#include "mxkern.cuh"
 
 namespace sgw {
 
-namespace {
-
-constexpr double kRoundRelThreshold = 1e-5;
-
-// |r|, r32 = r / |r| and the convergence flag, one CTA per right-hand side.
-__global__ void mx_normalise(int nrhs, int n, int npwx, const zcd* r, long long ldr, zcf* r32, double* scale,
-                             const double* bnorm, double target, int* active, int* nactive) {
-  __shared__ zcd red[32];
-  const int rhs = blockIdx.x;
-  if (rhs >= nrhs) return;
-  if (active[rhs] == 0) return;
-  const zcd* v = r + (size_t)rhs * ldr;
-  double p = 0.0;
-  for (int g = threadIdx.x; g < n; g += blockDim.x) p += abs2(v[g]);
-  const double nrm = sqrt(cta_sum(zcd{p, 0.0}, red).re);
-  const bool done = bnorm ? nrm <= target * bnorm[rhs] : false;
-  if (threadIdx.x == 0) {
-    scale[rhs] = nrm;
-    active[rhs] = done || nrm == 0.0 ? 0 : 1;
-    if (!done && nrm != 0.0) atomicAdd(nactive, 1);
-  }
-  const double inv = nrm > 0.0 ? 1.0 / nrm : 0.0;
-  zcf* o = r32 + (size_t)rhs * npwx;
-  for (int g = threadIdx.x; g < npwx; g += blockDim.x)
-    o[g] = g < n ? zcf{(float)(v[g].re * inv), (float)(v[g].im * inv)} : zcf{0.f, 0.f};
-}
-
-// x^sigma += scale Z^sigma y^sigma for active right-hand sides
-__global__ void mx_accumulate(int nrhs, int S, int n, int npwx, const zcf* y, zcd* x, long long ldx, long long ldr,
-                              const zcd* Z, const double* scale, const int* active, bool first) {
-  const long long total = (long long)nrhs * S * n;
-  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total; e += (long long)gridDim.x * blockDim.x) {
-    const int g = (int)(e % n);
-    const long long rs = e / n;
-    const int s = (int)(rs % S), rhs = (int)(rs / S);
-    zcd* dst = x + (size_t)rhs * ldr + (size_t)s * ldx + g;
-    if (!active[rhs]) {  // a zero right-hand side never becomes active: its solution is zero
-      if (first) *dst = zcd{0.0, 0.0};
-      continue;
-    }
-    const zcf yv = y[((size_t)rhs * S + s) * npwx + g];
-    const zcd f = scale[rhs] * Z[(size_t)rhs * S + s];
-    const zcd add = f * zcd{(double)yv.re, (double)yv.im};
-    *dst = first ? add : *dst + add;
-  }
-}
-
-__global__ void mx_update_z(int nrhs, int S, zcd* Z, const zcd* zeta, const int* active, int* iters_total,
-                            const int* iters_round) {
-  const int e = blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= nrhs * S) return;
-  const int rhs = e / S;
-  if (!active[rhs]) return;
-  Z[e] = Z[e] * zeta[e];
-  if (e % S == 0) iters_total[rhs] += iters_round[rhs];
-}
-
-__global__ void mx_init(int nrhs, int S, zcd* Z, int* active, int* iters_total) {
-  const int e = blockIdx.x * blockDim.x + threadIdx.x;
-  if (e < nrhs * S) Z[e] = zcd{1.0, 0.0};
-  if (e < nrhs) {
-    active[e] = 1;
-    iters_total[e] = 0;
-  }
-}
-
-// r = b - A(sigma_1) x_1 in FP64 for active right-hand sides; one CTA each.
-template <class ApplyT>
-__global__ void __launch_bounds__(CtaThreads<double>::v, 1)
-    mx_seed_residual(ApplyT A, int nrhs, int n, const zcd* bb, long long ldb, const zcd* sigma, long long lds,
-                     const zcd* x, long long ldr, zcd* r, long long ldrr, const int* active, zcd* col_global,
-                     long long col_slot) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  zcd* sm = reinterpret_cast<zcd*>(smem_raw);
-  zcd* col = A.col_in_smem ? sm + A.smem_small() : col_global + (size_t)blockIdx.x * col_slot;
-  A.setup(sm);
-  for (int rhs = blockIdx.x; rhs < nrhs; rhs += gridDim.x) {
-    if (!active[rhs]) continue;
-    zcd* out = r + (size_t)rhs * ldrr;
-    A.apply(x + (size_t)rhs * ldr, out, nullptr, sigma[(size_t)rhs * lds], sm, col);
-    const zcd* b = bb + (size_t)rhs * ldb;
-    for (int g = threadIdx.x; g < n; g += blockDim.x) out[g] = b[g] - out[g];
-    __syncthreads();
-  }
-}
-
-__global__ void mx_bnorm(int nrhs, int n, const zcd* bb, long long ldb, double* bnorm) {
-  __shared__ zcd red[32];
-  const int rhs = blockIdx.x;
-  if (rhs >= nrhs) return;
-  double p = 0.0;
-  for (int g = threadIdx.x; g < n; g += blockDim.x) p += abs2(bb[(size_t)rhs * ldb + g]);
-  const double s = sqrt(cta_sum(zcd{p, 0.0}, red).re);
-  if (threadIdx.x == 0) bnorm[rhs] = s;
-}
-
-__global__ void mx_finish(int nrhs, int S, int n, const zcd* x, long long ldx, long long ldr, const int* active,
-                          int* ierr, int max_rounds_hit) {
-  __shared__ int bad;
-  const int rhs = blockIdx.x;
-  if (rhs >= nrhs) return;
-  if (threadIdx.x == 0) bad = 0;
-  __syncthreads();
-  for (int e = threadIdx.x; e < S * n; e += blockDim.x) {
-    const zcd v = x[(size_t)rhs * ldr + (size_t)(e / n) * ldx + (e % n)];
-    if (v.re != v.re || v.im != v.im) bad = 1;
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) ierr[rhs] = bad ? 2 : (active[rhs] && max_rounds_hit ? 1 : 0);
-}
-
-}  // namespace
 
 sgw_status solve_mixed(sgw_operator* op, const BatchDev& b, int refine_max, double refine_thr) {
   const int R = b.nrhs, S = b.nshift, n = op->n, npwx = op->npwx;

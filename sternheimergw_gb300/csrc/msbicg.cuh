@@ -51,8 +51,8 @@ struct SolverArgs {
   int* iters;          // [rhs]
   int* counter;        // work queue head
   // per-CTA slot workspace
-  cplx<T>* ws_vec;     // [slot][nvec_slot][npwx]
-  long long nvec_slot;
+  cplx<T>* ws_vec;     // [slot][vec_stride]
+  long long vec_stride;  // elements per CTA slot (>= vectors needed x npwx)
   zcd* ws_coef;        // [slot][ncoef_slot]
   long long ncoef_slot;
   int Kcap;            // history vectors per window
@@ -391,7 +391,7 @@ __device__ void solve_one(const SolverArgs<T>& a, const ApplyT& A, int rhs, int 
   const int grows = max(1, gelems / a.P);
   const bool track = Sm1 > 0 && !explicit_mode;
 
-  cplx<T>* V = a.ws_vec + (size_t)slot * a.nvec_slot * npwx;
+  cplx<T>* V = a.ws_vec + (size_t)slot * a.vec_stride;
   cplx<T>* U = V;
   cplx<T>* R = V + (size_t)(l + 1) * npwx;
   cplx<T>* X = V + (size_t)(2 * l + 2) * npwx;

@@ -105,6 +105,14 @@ class _Operator:
         _capi.check(_capi.lib().sgw_kernel_timing(self.handle, int(kernel), C.byref(ms), C.byref(n)), "sgw_kernel_timing")
         return ms.value, n.value
 
+    def autotune(self, precision=0):
+        """Pick the fastest FFT launch shape of this operator's FP64 (0) or FP32 (1) kernels
+        (sgw_operator_autotune); returns a dict of the choice."""
+        r = _capi.TuneResult()
+        _capi.check(_capi.lib().sgw_operator_autotune(self.handle, int(precision), C.byref(r)), "sgw_operator_autotune")
+        return dict(lines=bool(r.lines), col_in_smem=bool(r.col_in_smem), planes=r.planes,
+                    us_per_apply=r.us_per_apply, candidates=r.candidates, cached=bool(r.cached))
+
     def last_timing(self):
         ms = C.c_double(0)
         n = C.c_int64(0)
@@ -419,3 +427,78 @@ def vjp(AA: PlaneWaveOperator, xx, lam, *, evc=None, nl_k=None, want_vloc=True, 
     d.ldx, d.ldr = n, S * n
     _capi.check(_capi.lib().sgw_vjp(AA.handle, C.byref(d)), "sgw_vjp")
     return gv, gd
+
+
+class MultiPlan:
+    """Uneven batch of independent systems solved together (sgw_multi_*).
+
+    systems: list of (operator, bb, sigma) with CUDA torch tensors bb (nrhs, n)
+    and sigma (nrhs, S) complex128.  Allocates the outputs x (nrhs, S, n),
+    ierr and iters per system; with use_graph the whole solve is captured once
+    as a CUDA graph and every run() replays it.
+    """
+
+    def __init__(self, systems, *, precision=1, lmax=4, threshold=1e-10, max_iter=10000, refine_max=0,
+                 refine_threshold=0.0, use_graph=True, history_iters=0):
+        import torch
+        self.ops = [s[0] for s in systems]
+        self.bb = [s[1].contiguous() for s in systems]
+        self.sigma = [s[2].contiguous() for s in systems]
+        self.x, self.ierr, self.iters = [], [], []
+        n = len(systems)
+        descs = (_capi.BatchDesc * n)()
+        for i, (op, bb, sg) in enumerate(zip(self.ops, self.bb, self.sigma)):
+            R, npw = bb.shape
+            S = sg.shape[1]
+            if npw != op.n or sg.shape[0] != R:
+                raise ValueError(f"system {i}: shapes do not match its operator")
+            x = torch.empty((R, S, npw), dtype=torch.complex128, device=bb.device)
+            ierr = torch.zeros(R, dtype=torch.int32, device=bb.device)
+            iters = torch.zeros(R, dtype=torch.int32, device=bb.device)
+            self.x.append(x)
+            self.ierr.append(ierr)
+            self.iters.append(iters)
+            d = descs[i]
+            d.nrhs, d.num_shift, d.lmax, d.max_iter = R, S, int(lmax), int(max_iter)
+            d.threshold = float(threshold)
+            d.precision = int(precision)
+            d.memory = 1
+            d.history_iters = int(history_iters)
+            d.bb, d.sigma, d.xx = bb.data_ptr(), sg.data_ptr(), x.data_ptr()
+            d.ierr, d.iters = ierr.data_ptr(), iters.data_ptr()
+            d.ldb, d.lds, d.ldx, d.ldr = npw, S, npw, S * npw
+        self._descs = descs
+        handles = (C.c_void_p * n)(*[op.handle.value if isinstance(op.handle, C.c_void_p) else op.handle
+                                     for op in self.ops])
+        o = _capi.MultiOptions()
+        o.precision, o.refine_max, o.refine_threshold, o.use_graph = (int(precision), int(refine_max),
+                                                                     float(refine_threshold), int(bool(use_graph)))
+        h = C.c_void_p()
+        _capi.check(_capi.lib().sgw_multi_create(n, handles, descs, C.byref(o), C.byref(h)), "sgw_multi_create")
+        self.handle = h
+        self.nsys = n
+
+    def run(self):
+        """Solve every system; returns (total_ms, per-system completion ms)."""
+        ms = C.c_double(0)
+        per = np.zeros(self.nsys, dtype=np.float64)
+        _capi.check(_capi.lib().sgw_multi_run(self.handle, C.byref(ms), per.ctypes.data), "sgw_multi_run")
+        return ms.value, per
+
+    def info(self):
+        n = C.c_int64(0)
+        g = C.c_int32(0)
+        gr = C.c_int32(0)
+        _capi.check(_capi.lib().sgw_multi_info(self.handle, C.byref(n), C.byref(g), C.byref(gr)), "sgw_multi_info")
+        return dict(launches_per_run=n.value, stage_launch_groups=g.value, graph=bool(gr.value))
+
+    def close(self):
+        if getattr(self, "handle", None):
+            _capi.lib().sgw_multi_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

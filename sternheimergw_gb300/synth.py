@@ -163,9 +163,18 @@ def lowest_states(h, nocc):
     return w[:nocc].copy(), np.asfortranarray(v)
 
 
+def dense_states(mill, nl, g2kin, vrs, nr, vkb, dvan, nocc):
+    """Lowest nocc eigenpairs of the dense FP64 H (numpy eigh)."""
+    return lowest_states(dense_h(mill, g2kin, vrs, nr, vkb, dvan), nocc)
+
+
 def make_system(alat, lattice, ecut, nocc, seed, nr=None, qvec=(0.1, 0.0, 0.0), n_pert=1,
-                kvec=(0.0, 0.0, 0.0)):
-    """Build one synthetic system (see module docstring)."""
+                kvec=(0.0, 0.0, 0.0), eigensolver=None):
+    """Build one synthetic system (see module docstring).
+
+    eigensolver(mill, nl, g2kin, vrs, nr, vkb, dvan, nocc) -> (eps, psi) gives
+    the occupied states (default: dense eigh); large systems pass an iterative
+    solver (sternheimergw_gb300.eigen)."""
     rng = np.random.default_rng(seed)
     if lattice == "fcc":
         avec, bmat, tau = _FCC_A, _FCC_B, np.array([[0, 0, 0], [0.25, 0.25, 0.25]])
@@ -191,13 +200,12 @@ def make_system(alat, lattice, ecut, nocc, seed, nr=None, qvec=(0.1, 0.0, 0.0), 
     tau_cart = tau * alat
     vkb_k, dvan = kb_projectors(rng, _cart(bmat, mill_k, k_float, alat), tau_cart, omega)
     vkb_kq, _ = kb_projectors(np.random.default_rng(0), _cart(bmat, mill_kq, kq_float, alat), tau_cart, omega)
-    h_k = dense_h(mill_k, g2_k, vrs, nr, vkb_k, dvan)
-    et, evc = lowest_states(h_k, nocc)
+    eig = eigensolver or dense_states
+    et, evc = eig(mill_k, nl_k, g2_k, vrs, nr, vkb_k, dvan, nocc)
     if np.array_equal(mill_k, mill_kq) and np.allclose(g2_k, g2_kq):
         evq = evc.copy(order="F")
     else:
-        h_kq = dense_h(mill_kq, g2_kq, vrs, nr, vkb_kq, dvan)
-        _, evq = lowest_states(h_kq, nocc)
+        _, evq = eig(mill_kq, nl_kq, g2_kq, vrs, nr, vkb_kq, dvan, nocc)
     alpha_pv = max(2.0 * (et.max() - et.min()), 1e-2)
     # perturbations: the n_pert G with smallest |q+G| (ties by Miller index)
     r = np.arange(-8, 9)
@@ -238,6 +246,47 @@ def omega_list(freq):
     if abs(freq[0]) < 1e-14:
         return np.concatenate([freq, -freq[1:]])
     return np.concatenate([freq, -freq])
+
+
+C3_SYSTEMS = 64
+C3_BASE_SEED = 3000
+
+
+def c3_params(index, base_seed=C3_BASE_SEED):
+    """Parameters of system `index` of the uneven batch: simple-cubic cell with 2
+    atoms at (0,0,0) and (1/4,1/4,1/4)a, a ~ U[8, 14] bohr, E_cut ~ U[12, 30] Ry,
+    bands ~ U{4..32}, perturbations ~ U{1..64}, frequencies ~ U{8..64}; the FFT
+    grid is the smooth grid of 4 E_cut kept within 24..48 per axis."""
+    rng = np.random.default_rng(base_seed + index)
+    a = float(rng.uniform(8.0, 14.0))
+    ecut = float(rng.uniform(12.0, 30.0))
+    nocc = int(rng.integers(4, 33))
+    npert = int(rng.integers(1, 65))
+    nfreq = int(rng.integers(8, 65))
+    need = fft_grid_for(a, _SC_A, 4 * ecut)[0]
+    n = good_fft_size(max(need, 24))
+    if n > 48:
+        n = 48
+    return dict(alat=a, ecut=ecut, nocc=nocc, npert=npert, nfreq=nfreq, nr=(n, n, n), seed=base_seed + index)
+
+
+def c3_freq(p):
+    """Half of the frequencies on the imaginary axis i [0, 60] eV, half on the real
+    axis x + 0.1 i eV with x ~ U[-30, 30] eV (sorted); omega_1 = 0."""
+    rng = np.random.default_rng(p["seed"] + 100000)
+    nf = p["nfreq"]
+    ni = nf // 2
+    im = 1j * np.linspace(0.0, 60.0, ni) / RY_EV
+    re = (np.sort(rng.uniform(-30.0, 30.0, nf - ni)) + 0.1j) / RY_EV
+    return np.concatenate([im, re])
+
+
+def c3_system(index, eigensolver=None, base_seed=C3_BASE_SEED):
+    """System `index` of the uneven batch and its frequency list."""
+    p = c3_params(index, base_seed)
+    s = make_system(p["alat"], "sc2", p["ecut"], p["nocc"], p["seed"], nr=p["nr"], n_pert=p["npert"],
+                    eigensolver=eigensolver)
+    return s, c3_freq(p)
 
 
 def config(name: str, seed: int | None = None):
