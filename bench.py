@@ -319,6 +319,93 @@ def w_error_imag_axis():
     return norm, elem, int(max(e64.max(), em.max()))
 
 
+def run_c3(steps=2, warmup=1, sequential=True):
+    """Uneven batch of 64 independent systems (simple-cubic 2-atom cells, a in [8, 14] bohr,
+    E_cut in [12, 30] Ry, 24^3..48^3 boxes, 4..32 bands, 1..64 perturbations, 8..64
+    frequencies half imaginary / half real): mixed precision, one persistent launch per
+    stage over all systems, captured as a CUDA graph; FFT shapes from the autotuner.
+    Reports aggregate solves/s, per-system completion p50/p99, and the same systems
+    solved one after another with sgw_solve_batch for comparison."""
+    import torch
+
+    import sternheimergw_gb300 as sg
+    from sternheimergw_gb300 import eigen, linter, synth
+    free, total_mem = torch.cuda.mem_get_info()
+    t0 = time.time()
+    specs = [synth.c3_system(i, eigensolver=eigen.lowest_states_gpu) for i in range(synth.C3_SYSTEMS)]
+    t_gen = time.time() - t0
+    t1 = time.time()
+    ops, bbs, sigs, meta = [], [], [], []
+    tunes = []
+    for s, f in specs:
+        op = sg.PlaneWaveOperator(s)
+        tunes.append((op.autotune(0), op.autotune(1)))
+        bbs.append(linter.coulomb_rhs(op, s, device=True))
+        sig = np.tile(linter.coulomb_shifts(s, f), (len(s["gpert"]), 1))
+        sigs.append(torch.from_numpy(sig).cuda())
+        ops.append(op)
+        meta.append(dict(npw=int(s["npw"]), nr=int(s["nr"][0]), nocc=int(s["nocc"]), npert=len(s["gpert"]),
+                         shifts=int(sig.shape[1])))
+    t_setup = time.time() - t1
+    solves = int(sum(b.shape[0] * g.shape[1] for b, g in zip(bbs, sigs)))
+    out_bytes = sum(b.shape[0] * g.shape[1] * b.shape[1] * 16 for b, g in zip(bbs, sigs))
+    log(f"[bench-c3] {len(specs)} systems generated in {t_gen:.1f}s, set up in {t_setup:.1f}s: "
+        f"{sum(b.shape[0] for b in bbs)} RHS, {solves} solves, outputs {out_bytes / 1e9:.1f} GB")
+    seq = None
+    if sequential:
+        xs = [torch.empty((b.shape[0], g.shape[1], b.shape[1]), dtype=torch.complex128, device="cuda")
+              for b, g in zip(bbs, sigs)]
+        done, tsum = [], 0.0
+        for op, b, g, x in zip(ops, bbs, sigs, xs):
+            # untimed call first (allocates the handle's buffers), then the timed one; buffers
+            # are released afterwards so that 64 handles' scratch never coexists
+            sg.solve_batch(op, b, g, lmax=LMAX, threshold=THRESHOLD, precision=1, out=x)
+            sg.solve_batch(op, b, g, lmax=LMAX, threshold=THRESHOLD, precision=1, out=x)
+            tsum += op.last_timing()[0]
+            done.append(tsum)
+            op.trim()
+        seq = dict(total_ms=tsum, solves_per_s=solves / (tsum * 1e-3),
+                   p50_ms=float(np.percentile(done, 50)), p99_ms=float(np.percentile(done, 99)))
+        log(f"[bench-c3] one system after another: {tsum:.1f} ms")
+        del xs
+        torch.cuda.empty_cache()
+    plan = sg.solver.MultiPlan(list(zip(ops, bbs, sigs)), precision=1, lmax=LMAX, threshold=THRESHOLD,
+                               use_graph=True)
+    for _ in range(warmup):
+        plan.run()
+    runs, lat = [], []
+    for _ in range(steps):
+        ms, per = plan.run()
+        runs.append(ms)
+        lat.append(per)
+        log(f"[bench-c3] batched run: {ms:.1f} ms")
+    info = plan.info()
+    ierr_max = max(int(e.max().item()) for e in plan.ierr)
+    ms = float(np.median(runs))
+    per = lat[int(np.argsort(runs)[len(runs) // 2])]
+    shapes = {}
+    for m, (t64, t32) in zip(meta, tunes):
+        shapes.setdefault(m["nr"], (t64["lines"], t64["planes"], t32["lines"], t32["planes"]))
+    res = {
+        "systems": len(specs), "rhs": int(sum(b.shape[0] for b in bbs)), "solves": solves,
+        "npw_range": [min(m["npw"] for m in meta), max(m["npw"] for m in meta)],
+        "grids": sorted({m["nr"] for m in meta}),
+        "value": solves / (ms * 1e-3), "unit": "solves/s", "ms_per_run": ms,
+        "p50_ms": float(np.percentile(per, 50)), "p99_ms": float(np.percentile(per, 99)),
+        "launches_per_run": info["launches_per_run"], "persistent_groups_per_stage": info["stage_launch_groups"],
+        "cuda_graph": info["graph"], "ierr_max": ierr_max, "precision": "mixed",
+        "sequential": seq,
+        "autotuned_shapes_by_grid": {str(k): {"fp64_lines": v[0], "fp64_planes": v[1], "fp32_lines": v[2],
+                                              "fp32_planes": v[3]} for k, v in sorted(shapes.items())},
+        "generation_s": t_gen, "setup_s": t_setup,
+        "gpu_mem_free_gb_before": free / 1e9,
+    }
+    plan.close()
+    for op in ops:
+        op.close()
+    return res
+
+
 def run_gpu(args, rank, world):
     import torch
     import torch.distributed as dist
@@ -412,6 +499,10 @@ def run_gpu(args, rank, world):
     h2d = bb.nbytes + sigma.nbytes
     d2h = nrhs * S * n * 16 + nrhs * 8
 
+    c3 = None
+    if not args.no_c3:
+        c3 = run_c3()
+
     out = None
     if rank == 0:
         peak64 = fp64_peak_tflops()
@@ -467,6 +558,7 @@ def run_gpu(args, rank, world):
                         "average fused), timed outside the solve steps"},
             "mixed_kernel_ms_per_step": {"fp32_solve": k32_ms / args.steps, "fp64_seed_residual": kres_ms / args.steps,
                                          "total": ms_m},
+            "uneven_batch": c3,
             "cpu_baseline": {"value": cpu_v, "unit": "solves/s", "cores": os.cpu_count() or 1, "kind": "port",
                              "sample": f"{sample} of {nrhs} right-hand sides x {S} shifts, {cpu_dt:.1f}s"},
             "gpu_launches": int(pm["launches"]),
@@ -486,6 +578,8 @@ def main():
     ap.add_argument("--nrhs", type=int, default=0,
                     help="solve only the first N right-hand sides (reduced case for profiling; 0 = all)")
     ap.add_argument("--precision", default="both", choices=["both", "fp64", "mixed"])
+    ap.add_argument("--no-c3", action="store_true", help="skip the uneven 64-system batch")
+    ap.add_argument("--c3-only", action="store_true", help="run only the uneven 64-system batch and print it")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the e2e leg, the W-error check, the peak probes and the CPU baseline (profiling runs)")
     args = ap.parse_args()
@@ -500,6 +594,16 @@ def main():
         dist.init_process_group(backend)
     if args.impl == "reference":
         run_reference(args, rank, world)
+    elif args.c3_only:
+        import torch
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+        from sternheimergw_gb300 import _capi
+        _capi.lib(build_if_missing=False)
+        with ClockSampler(int(os.environ.get("LOCAL_RANK", 0))) as clk:
+            r = run_c3(steps=args.steps, warmup=max(1, min(args.warmup, 2)))
+        r["clocks"] = clk.summary()
+        if rank == 0:
+            print(json.dumps({"uneven_batch": r}), flush=True)
     else:
         run_gpu(args, rank, world)
     if world > 1:

@@ -90,6 +90,12 @@ sgw_status sgw_operator_create_dense(int32_t n, const sgw_zcomplex* a, int64_t l
 
 sgw_status sgw_operator_destroy(sgw_operator* op);
 
+/* Release the handle's scratch and staging buffers (they are allocated again,
+ * at the size needed, by the next call that uses them); the operator tables
+ * stay.  No counterpart in the reference, whose solver frees its state on
+ * every return (bicgstab.f90:272-273). */
+sgw_status sgw_operator_trim(sgw_operator* op);
+
 /* Switch between the Coulomb operator (alpha_pv from the set-up,
  * solve_linter.f90:657-716) and the Green's-function operator (alpha_pv = 0,
  * green.f90:231-291) without rebuilding the handle. */

@@ -551,6 +551,18 @@ sgw_status sgw_operator_destroy(sgw_operator* op) {
   return SGW_OK;
 }
 
+sgw_status sgw_operator_trim(sgw_operator* op) {
+  if (!op) return arg_error("null operator");
+  if (op->stream) SGW_CK(cudaStreamSynchronize(op->stream));
+  DevBuf* bufs[] = {&op->ws64.vec, &op->ws64.coef, &op->ws64.col, &op->ws64.counter, &op->ws32.vec, &op->ws32.coef,
+                    &op->ws32.col, &op->ws32.counter, &op->st_bb, &op->st_sigma, &op->st_xx, &op->st_ierr,
+                    &op->st_iters, &op->st_misc, &op->st_misc2, &op->st_misc3, &op->lt_psi, &op->lt_box,
+                    &op->lt_nlk, &op->lt_evc, &op->lt_dv, &op->lt_bb, &op->lt_flag, &op->lt_part, &op->lt_sidx,
+                    &op->lt_xx, &op->lt_chi};
+  for (DevBuf* b : bufs) b->release();
+  return SGW_OK;
+}
+
 sgw_status sgw_operator_set_alpha_pv(sgw_operator* op, double alpha_pv) {
   if (!op) return arg_error("null operator");
   op->alpha_pv = alpha_pv;

@@ -85,6 +85,10 @@ class _Operator:
         except Exception:
             pass
 
+    def trim(self):
+        """Release the handle's scratch and staging buffers (sgw_operator_trim)."""
+        _capi.check(_capi.lib().sgw_operator_trim(self.handle), "sgw_operator_trim")
+
     def set_alpha_pv(self, alpha_pv: float):
         _capi.check(_capi.lib().sgw_operator_set_alpha_pv(self.handle, float(alpha_pv)), "sgw_operator_set_alpha_pv")
 
