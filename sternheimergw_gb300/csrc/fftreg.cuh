@@ -77,16 +77,20 @@ __device__ __forceinline__ void fft_reg(cplx<T>* v, const cplx<T>* tw) {
 // registers: up to 48 complex floats or 40 complex doubles).
 template <typename T>
 __host__ __device__ constexpr bool fft_reg_supported(int n) {
-  return n == 20 || n == 24 || n == 30 || n == 32 || n == 36 || n == 40 ||
-         (sizeof(T) == 4 && (n == 45 || n == 48));
+  return n == 16 || n == 18 || n == 20 || n == 24 || n == 25 || n == 27 || n == 30 || n == 32 || n == 36 ||
+         n == 40 || (sizeof(T) == 4 && (n == 45 || n == 48));
 }
 
 // Call f(std::integral_constant<int, N>) for the supported runtime length n.
 template <typename T, class F>
 __device__ __forceinline__ void with_len(int n, F&& f) {
   switch (n) {
+    case 16: f(std::integral_constant<int, 16>{}); break;
+    case 18: f(std::integral_constant<int, 18>{}); break;
     case 20: f(std::integral_constant<int, 20>{}); break;
     case 24: f(std::integral_constant<int, 24>{}); break;
+    case 25: f(std::integral_constant<int, 25>{}); break;
+    case 27: f(std::integral_constant<int, 27>{}); break;
     case 30: f(std::integral_constant<int, 30>{}); break;
     case 32: f(std::integral_constant<int, 32>{}); break;
     case 36: f(std::integral_constant<int, 36>{}); break;

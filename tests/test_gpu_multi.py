@@ -1,5 +1,6 @@
 """Uneven batches (sgw_multi_*): systems of different G-spheres, FFT boxes
-(20^3 and 24^3 with the register-line FFT, 25^3 with the shared-memory FFT),
+(20^3, 24^3 and 27x27x25 with the register-line FFT, 25x25x50 with the
+shared-memory FFT),
 bands, perturbations and shift counts in one persistent launch per stage.
 Each system's solution must equal what sgw_solve_batch gives for that system
 alone (same kernels and per-RHS arithmetic: 1e-13 relative), with and without
@@ -25,8 +26,9 @@ def systems(gpu_lib):
     out = []
     specs = [(synth.config("c0")[0], synth.freq_imag(10, 50.0)),
              (synth.make_system(8.0, "sc2", 12.0, 5, 71, nr=(24, 24, 24), n_pert=3), synth.freq_imag(7, 60.0)),
-             (synth.make_system(8.3, "sc2", 13.0, 4, 72, nr=(25, 25, 25), n_pert=2),
-              np.concatenate([synth.freq_imag(4, 60.0), (np.array([-5.0, 3.0, 11.0]) + 0.1j) / synth.RY_EV]))]
+             (synth.make_system(8.3, "sc2", 13.0, 4, 72, nr=(25, 25, 50), n_pert=2),
+              np.concatenate([synth.freq_imag(4, 60.0), (np.array([-5.0, 3.0, 11.0]) + 0.1j) / synth.RY_EV])),
+             (synth.make_system(8.1, "sc2", 12.5, 3, 74, nr=(27, 27, 25), n_pert=2), synth.freq_imag(5, 60.0))]
     for s, f in specs:
         op = sg.PlaneWaveOperator(s)
         bb = linter.coulomb_rhs(op, s, device=True)
@@ -58,7 +60,7 @@ def test_multi_matches_single(systems, precision, use_graph):
 
 
 def test_multi_solution_vs_oracle(systems):
-    """The shared-memory-FFT system (25^3) of the batch against the oracle solver."""
+    """The shared-memory-FFT system (25x25x50) of the batch against the oracle solver."""
     s, f, op, bb, sh = systems[2]
     plan = sg.solver.MultiPlan([(o, b, h) for _, _, o, b, h in systems], precision=0, threshold=1e-10)
     plan.run()
@@ -100,3 +102,13 @@ def test_lobpcg_states_match_dense(gpu_lib):
     wd, vd = synth.dense_states(*args)
     assert np.abs(w - wd).max() < 1e-9
     assert np.linalg.norm(v @ v.conj().T - vd @ vd.conj().T) < 1e-6
+
+
+def test_new_register_lengths_apply_parity(systems):
+    """Boxes of 27 and 25 points per axis run the register-line FFT (FP64 apply vs oracle)."""
+    s, f, op, bb, sh = systems[3]
+    rng = np.random.default_rng(8)
+    v = rng.standard_normal(op.n) + 1j * rng.standard_normal(op.n)
+    got = op.apply(-0.2 + 0.3j, v)
+    ref = O.apply(O.PlaneWaveOperator(s), -0.2 + 0.3j, v)
+    assert rel(got, ref) < 1e-13
