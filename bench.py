@@ -406,6 +406,52 @@ def run_c3(steps=2, warmup=1, sequential=True):
     return res
 
 
+def run_caller(args):
+    """Profiling case for the kernels around the solve: the right-hand sides of the
+    large system (sgw_coulomb_rhs), one mixed solve of the first --nrhs of them,
+    the density response of those solutions (sgw_chi), and one adjoint solve plus
+    the vector-Jacobian products on the imaginary-axis system (sgw_solve_adjoint,
+    sgw_vjp).  Prints the CUDA-event time of each call."""
+    import torch
+
+    import sternheimergw_gb300 as sg
+    from sternheimergw_gb300 import linter, synth
+    holder = {}
+
+    def make_op(system):
+        holder["op"] = sg.PlaneWaveOperator(system)
+        return holder["op"]
+
+    s, f, bb, sigma, bb_d = make_workload(make_op)
+    op = holder["op"]
+    rhs_ms = op.kernel_timing(3)[0]
+    nocc = s["nocc"]
+    nrhs = args.nrhs or bb.shape[0]
+    nrhs -= nrhs % nocc
+    bb_d = bb_d[:nrhs].contiguous()
+    sg_d = torch.from_numpy(sigma[:nrhs]).cuda()
+    x, ierr, _ = sg.solve_batch(op, bb_d, sg_d, lmax=LMAX, threshold=THRESHOLD, precision=1)
+    linter.chi_matrix(op, bb_d, x, nocc, f)
+    chi_ms = op.kernel_timing(4)[0]
+    s4, f4 = synth.config("c4")
+    op4 = sg.PlaneWaveOperator(s4)
+    b4 = linter.coulomb_rhs(op4, s4, device=True)
+    sh4 = torch.from_numpy(np.tile(linter.coulomb_shifts(s4, f4), (len(s4["gpert"]), 1))).cuda()
+    x4, _, _ = sg.solve_batch(op4, b4, sh4, lmax=LMAX, threshold=THRESHOLD)
+    g = torch.randn(x4.shape, dtype=torch.complex128, device="cuda")
+    lam, _ = sg.solver.solve_adjoint(op4, g, sh4, threshold=THRESHOLD)
+    adj_ms = op4.last_timing()[0]
+    evc = torch.from_numpy(np.ascontiguousarray(np.asarray(s4["evc"]).T)).cuda()
+    nlk = torch.from_numpy(np.ascontiguousarray(s4["nl_k"], dtype=np.int32)).cuda()
+    sg.solver.vjp(op4, x4, lam, evc=evc, nl_k=nlk)
+    vjp_ms = op4.kernel_timing(5)[0]
+    out = {"caller_profile": True, "rhs_built": int(bb.shape[0]), "rhs_ms": rhs_ms, "chi_rhs": nrhs,
+           "chi_ms": chi_ms, "adjoint_systems": int(x4.shape[0] * x4.shape[1]), "adjoint_ms": adj_ms,
+           "vjp_ms": vjp_ms, "ierr_max": int(ierr.max().item())}
+    print(json.dumps(out), flush=True)
+    return out
+
+
 def run_gpu(args, rank, world):
     import torch
     import torch.distributed as dist
@@ -580,6 +626,8 @@ def main():
     ap.add_argument("--precision", default="both", choices=["both", "fp64", "mixed"])
     ap.add_argument("--no-c3", action="store_true", help="skip the uneven 64-system batch")
     ap.add_argument("--c3-only", action="store_true", help="run only the uneven 64-system batch and print it")
+    ap.add_argument("--caller-only", action="store_true",
+                    help="profiling case: right-hand sides, one mixed solve of --nrhs, chi, adjoint + VJP")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the e2e leg, the W-error check, the peak probes and the CPU baseline (profiling runs)")
     args = ap.parse_args()
@@ -594,6 +642,12 @@ def main():
         dist.init_process_group(backend)
     if args.impl == "reference":
         run_reference(args, rank, world)
+    elif args.caller_only:
+        import torch
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+        from sternheimergw_gb300 import _capi
+        _capi.lib(build_if_missing=False)
+        run_caller(args)
     elif args.c3_only:
         import torch
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))

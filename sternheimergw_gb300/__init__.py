@@ -8,8 +8,8 @@ from .solver import (BICGSTAB_MULTI, BICGSTAB_NO_MULTI, SGW_LINEAR_SOLVER, Bicgs
                      LinearSolverConfig, PlaneWaveOperator, SelectSolverConfig, bicgstab, linear_solver,
                      select_solver, solve_batch)
 from ._capi import SgwError
-from . import solver
+from . import linter, solver
 
 __all__ = ["BICGSTAB_MULTI", "BICGSTAB_NO_MULTI", "SGW_LINEAR_SOLVER", "BicgstabConfig", "DenseOperator",
            "LinearSolverConfig", "PlaneWaveOperator", "SelectSolverConfig", "bicgstab", "linear_solver",
-           "select_solver", "solve_batch", "SgwError", "solver"]
+           "select_solver", "solve_batch", "SgwError", "solver", "linter"]
