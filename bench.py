@@ -471,6 +471,8 @@ def run_gpu(args, rank, world):
     s, f, bb, sigma, bb_d = make_workload(make_op)
     op = holder["op"]
     rhs_ms = op.kernel_timing(3)[0]
+    tuned = {"fp64": op.autotune(0), "fp32": op.autotune(1)}
+    log(f"[bench] autotuned FFT shapes: {tuned}")
     if args.nrhs:
         bb, sigma, bb_d = bb[:args.nrhs], sigma[:args.nrhs], bb_d[:args.nrhs].contiguous()
     nrhs, S = sigma.shape
@@ -570,7 +572,9 @@ def run_gpu(args, rank, world):
                        "precision": "mixed (headline) and fp64", "refine_target": 1e-9,
                        "l2": "256 MB buffer written between steps; outputs 4.6 GB > L2",
                        "mean_fp32_iterations": float(np.mean(pm["iters"])),
-                       "mean_fp64_iterations": float(np.mean(p64["iters"]))},
+                       "mean_fp64_iterations": float(np.mean(p64["iters"])),
+                       "fft_shapes_autotuned": {k: {"register_lines": v["lines"], "planes_in_flight": v["planes"],
+                                                    "columns_in_smem": v["col_in_smem"]} for k, v in tuned.items()}},
             "plain_fp64": {"value": value64, "unit": "solves/s", "ms_per_step": ms_64,
                            "ierr_max": int(p64["ierr"].max())},
             "speedup_mixed_vs_fp64": value / value64,

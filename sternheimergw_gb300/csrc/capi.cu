@@ -58,9 +58,10 @@ static void twiddles(int n, std::vector<cplx<T>>& out) {
 // Launch-shape selection
 // ---------------------------------------------------------------------------
 template <typename T>
-static PwShape choose_shape(const PwView<T>& v, size_t smem_optin) {
+static PwShape choose_shape(const PwView<T>& v, size_t smem_optin, size_t smem_per_sm) {
   const size_t static_bytes = sizeof(SeedShared) + 64;
-  const size_t budget = smem_optin > static_bytes ? smem_optin - static_bytes : 0;
+  const size_t per_cta = std::min(smem_optin, smem_per_sm / CtasPerSm<T>::v - 1024);
+  const size_t budget = per_cta > static_bytes ? per_cta - static_bytes : 0;
   const size_t colb = (size_t)v.ncol * v.ldz * sizeof(cplx<T>);
   auto small = [&](int ng) { return (size_t)pw_smem_small(v, ng) * sizeof(cplx<T>); };
   PwShape s;
@@ -109,6 +110,7 @@ static sgw_status init_common(sgw_operator* op) {
   SGW_CK(cudaGetDeviceProperties(&prop, op->device));
   op->num_sms = prop.multiProcessorCount;
   op->smem_optin = prop.sharedMemPerBlockOptin;
+  op->smem_per_sm = prop.sharedMemPerMultiprocessor;
   SGW_CK(cudaStreamCreateWithFlags(&op->stream, cudaStreamNonBlocking));
   SGW_CK(cudaEventCreate(&op->ev0));
   SGW_CK(cudaEventCreate(&op->ev1));
@@ -184,6 +186,9 @@ static sgw_status upload_pw(sgw_operator* op, const sgw_pw_operator_desc* d, con
   v.g_i3 = op->gi3.as<int>();
   v.col_pos = op->colpos.as<int>();
   v.i1_list = op->i1list.as<int>();
+  v.ymask = op->ymask.as<unsigned long long>();
+  v.xmask = op->xmask;
+  v.zmask = op->zmask.as<unsigned long long>();
   v.g2kin = g2k.as<T>();
   v.vrs = vrs.as<T>();
   v.nkb = d->nkb;
@@ -196,7 +201,7 @@ static sgw_status upload_pw(sgw_operator* op, const sgw_pw_operator_desc* d, con
   v.p2 = p2;
   v.p3 = p3;
   v.tw = tw.as<cplx<T>>();
-  pwshape<T>(op) = choose_shape(v, op->smem_optin);
+  pwshape<T>(op) = choose_shape(v, op->smem_optin, op->smem_per_sm);
   return SGW_OK;
 }
 
@@ -266,6 +271,22 @@ static sgw_status create_pw(const sgw_pw_operator_desc* d, sgw_operator** out) {
   if (s == SGW_OK) s = op->gi3.upload(gi3.data(), gi3.size());
   if (s == SGW_OK) s = op->colpos.upload(colpos.data(), colpos.size());
   if (s == SGW_OK) s = op->i1list.upload(i1v.data(), i1v.size());
+  if (s == SGW_OK) {
+    // column masks of the register-line apply: i2 positions per listed i1, and the listed i1
+    std::vector<unsigned long long> ym(i1v.size(), 0ull);
+    op->xmask = 0ull;
+    for (size_t l = 0; l < i1v.size(); ++l) op->xmask |= 1ull << i1v[l];
+    for (int k = 0; k < ncol; ++k) {
+      const size_t l = std::lower_bound(i1v.begin(), i1v.end(), cols[k].second) - i1v.begin();
+      ym[l] |= 1ull << cols[k].first;
+    }
+    s = op->ymask.upload(ym.data(), ym.size());
+  }
+  if (s == SGW_OK) {
+    std::vector<unsigned long long> zm(ncol, 0ull);
+    for (int g = 0; g < d->npw; ++g) zm[gcol[g]] |= 1ull << gi3[g];
+    s = op->zmask.upload(zm.data(), zm.size());
+  }
   if (s == SGW_OK)
     s = upload_pw<double>(op, d, gcol, gi3, colpos, i1v, ncol, ldz, pitch, p1, p2, p3, op->g2k64, op->vrs64,
                           op->vkb64, op->dvan64, op->evq64, op->tw64);
@@ -383,7 +404,10 @@ static sgw_status solve_batch(sgw_operator* op, const sgw_batch_desc* d) {
     b.iters = op->st_iters.as<int>();
     s = solve_batch_device(op, b, d->precision, d->refine_max, d->refine_threshold);
     if (s != SGW_OK) return s;
-    if (d->ldr == (long long)S * d->ldx) {  // one copy: every (rhs, shift) row at a uniform host pitch
+    if (d->ldx == n && d->ldr == (long long)S * n) {  // packed host array: one linear copy
+      SGW_CK(cudaMemcpyAsync(d->xx, op->st_xx.p, sizeof(zcd) * (size_t)R * S * n, cudaMemcpyDeviceToHost,
+                             op->stream));
+    } else if (d->ldr == (long long)S * d->ldx) {  // one copy: every (rhs, shift) row at a uniform host pitch
       SGW_CK(cudaMemcpy2DAsync(d->xx, sizeof(zcd) * d->ldx, op->st_xx.p, sizeof(zcd) * n, sizeof(zcd) * n,
                                (size_t)R * S, cudaMemcpyDeviceToHost, op->stream));
     } else {
@@ -532,7 +556,7 @@ sgw_status sgw_operator_create_dense(int32_t n, const sgw_zcomplex* a, int64_t l
 sgw_status sgw_operator_destroy(sgw_operator* op) {
   if (!op) return SGW_OK;
   if (op->stream) cudaStreamSynchronize(op->stream);
-  DevBuf* bufs[] = {&op->gcol, &op->gi3, &op->colpos, &op->i1list, &op->g2k64, &op->g2k32, &op->vrs64, &op->vrs32,
+  DevBuf* bufs[] = {&op->ymask, &op->zmask, &op->gcol, &op->gi3, &op->colpos, &op->i1list, &op->g2k64, &op->g2k32, &op->vrs64, &op->vrs32,
                     &op->vkb64, &op->vkb32, &op->dvan64, &op->dvan32, &op->evq64, &op->evq32, &op->tw64, &op->tw32,
                     &op->a64, &op->a32, &op->ws64.vec, &op->ws64.coef, &op->ws64.col, &op->ws64.counter,
                     &op->ws32.vec, &op->ws32.coef, &op->ws32.col, &op->ws32.counter, &op->st_bb, &op->st_sigma,

@@ -94,7 +94,7 @@ struct sgw_operator {
   int kind = 0;  // 0 dense, 1 plane-wave
   int n = 0, npwx = 0;
   int device = 0, num_sms = 0;
-  size_t smem_optin = 0;
+  size_t smem_optin = 0, smem_per_sm = 0;
   cudaStream_t stream = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   cudaEvent_t lev0 = nullptr, lev1 = nullptr;  // sgw_coulomb_rhs / sgw_chi timing
@@ -108,7 +108,8 @@ struct sgw_operator {
   long long kernel_launches[sgw::K_NUM] = {};
   double alpha_pv = 0.0;
   // tables
-  sgw::DevBuf nlkq, gcol, gi3, colpos, i1list, g2k64, g2k32, vrs64, vrs32, vkb64, vkb32, dvan64, dvan32, evq64, evq32,
+  unsigned long long xmask = 0;
+  sgw::DevBuf nlkq, ymask, zmask, gcol, gi3, colpos, i1list, g2k64, g2k32, vrs64, vrs32, vkb64, vkb32, dvan64, dvan32, evq64, evq32,
       tw64, tw32, a64, a32;
   sgw::PwView<double> pw64{};
   sgw::PwView<float> pw32{};

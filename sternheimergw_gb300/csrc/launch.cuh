@@ -41,7 +41,7 @@ sgw_status run_msbicg(sgw_operator* op, const BatchDev& b) {
   // coefficient form loses accuracy through cancellation for l > 8)
   const int mode = l > 8 ? 1 : 0;
   const int Kcap = (Sm1 > 0 && mode == 0) ? Db * Tw : 0;
-  const int nslots = std::max(1, std::min(b.nrhs, op->num_sms));
+  const int nslots = std::max(1, std::min(b.nrhs, op->num_sms * CtasPerSm<T>::v));
   const long long nvec_slot = (2LL * l + 4) + (mode == 0 ? Kcap + (Sm1 > 0 ? Sm1 : 0) : (long long)Sm1 * (l + 2));
   const CoefLayout L(l, P, Kcap);
   Workspace& ws = wsp<T>(op);
@@ -112,7 +112,7 @@ sgw_status run_sgw(sgw_operator* op, const SgwArgs<T>& a) {
 
 template <typename T>
 sgw_status run_apply(sgw_operator* op, int m, const cplx<T>* x, long long ldi, cplx<T>* ax, long long ldo, zcd sigma) {
-  const int grid = std::min(m, op->num_sms);
+  const int grid = std::min(m, op->num_sms * CtasPerSm<T>::v);
   const long long colsz = col_elems<T>(op);
   Workspace& ws = wsp<T>(op);
   if (op->kind == 1 && !pwshape<T>(op).col_in_smem) {
@@ -163,7 +163,7 @@ sgw_status run_msbicg_in(sgw_operator* op, const BatchDev& b, unsigned char* reg
       continue;
     }
     const int fit = (int)std::min<size_t>((region_bytes - head - iters_bytes) / per_slot, (size_t)1 << 20);
-    const int nslots = std::max(1, std::min(std::min(b.nrhs, op->num_sms), fit));
+    const int nslots = std::max(1, std::min(std::min(b.nrhs, op->num_sms * CtasPerSm<T>::v), fit));
     unsigned char* p = region + head;
     SolverArgs<T> a{};
     a.counter = reinterpret_cast<int*>(region);

@@ -33,7 +33,12 @@ namespace sgw {
 constexpr int kMaxL = 16;
 // CTA size: 256 threads, so a thread may hold up to 255 registers (a whole
 // FFT line in the register path).
+// Solver CTAs: 256 threads, one per SM, in both precisions.  (Two 128-thread
+// FP32 CTAs per SM - same register budget per thread, half the shared memory
+// each - measured 11% slower on the production system: the apply throughput
+// per SM did not change and the CTA-wide vector work got slower.)
 template <typename T> struct CtaThreads { static constexpr int v = 256; };
+template <typename T> struct CtasPerSm { static constexpr int v = 1; };
 constexpr int kThreads = 512;
 
 template <typename T>
@@ -115,7 +120,7 @@ struct PwApply {
   // shared memory the basis product may use once the applies are done (the plane buffers)
   __device__ cplx<T>* scratch(cplx<T>* sm, int& elems) const {
     elems = ng * op.nr2 * op.pitch;
-    return sm + op.nr1 + op.nr2 + op.nr3 + op.nkb + op.nocc;
+    return sm + op.nr1 + op.nr2 + op.nr3 + op.nkb + op.nocc + pw_cpos_units(op);
   }
   __device__ void setup(cplx<T>* sm) const {
     for (int e = threadIdx.x; e < op.nr1 + op.nr2 + op.nr3; e += blockDim.x) sm[e] = op.tw[e];
@@ -311,14 +316,20 @@ __device__ __forceinline__ void replay_window_cta(zcd* C, const CoefLayout& L, i
 template <typename T>
 struct GemmShape {
   static constexpr int GL = 128;                        // rows per tile
-  static constexpr int QMAX = sizeof(T) == 4 ? 36 : 16; // shifts per thread per pass
+  static constexpr int RB = 2;                          // rows per thread (register blocking)
+  static constexpr int QMAX = sizeof(T) == 4 ? 18 : 8;  // shifts per thread per pass
 };
 
+// y[s][g] (+)= sum_k W[k][g] C[k][s] (+ carry[s] Z[s][g]) for g < n, s < ns.
+// Threads form (GL/RB) row lanes x (blockDim*RB/GL) shift groups; each thread
+// keeps RB rows x QMAX shifts of accumulators, so every coefficient read from
+// shared memory feeds RB complex FMAs and every W element QMAX of them.
 template <typename T>
 __device__ void cta_basis_gemm(cplx<T>* y, long long ldy, bool accumulate, const cplx<T>* W, int K, const zcd* C,
                                int P, const zcd* carry, const cplx<T>* Z, int ns, int n, int npwx, zcd* cvt,
                                cplx<T>* smbuf, int smrows) {
-  constexpr int GL = GemmShape<T>::GL, QMAX = GemmShape<T>::QMAX;
+  constexpr int GL = GemmShape<T>::GL, RB = GemmShape<T>::RB, QMAX = GemmShape<T>::QMAX;
+  constexpr int GR = GL / RB;  // row lanes
   const cplx<T>* Ck;
   if constexpr (sizeof(T) == 8) {
     Ck = reinterpret_cast<const cplx<T>*>(C);
@@ -328,8 +339,8 @@ __device__ void cta_basis_gemm(cplx<T>* y, long long ldy, bool accumulate, const
     __syncthreads();
     Ck = c32;
   }
-  const int sgrp = blockDim.x / GL;
-  const int gl = threadIdx.x % GL, sg = threadIdx.x / GL;
+  const int sgrp = blockDim.x / GR;
+  const int gl = threadIdx.x % GR, sg = threadIdx.x / GR;
   const bool whole = K <= smrows;
   auto fill = [&](int k0, int kc) {
     __syncthreads();
@@ -339,32 +350,45 @@ __device__ void cta_basis_gemm(cplx<T>* y, long long ldy, bool accumulate, const
   if (whole) fill(0, K);
   for (int s0 = 0; s0 < ns; s0 += sgrp * QMAX) {
     for (int g0 = 0; g0 < n; g0 += GL) {
-      const int g = g0 + gl;
-      cplx<T> acc[QMAX];
+      cplx<T> acc[RB][QMAX];
 #pragma unroll
-      for (int q = 0; q < QMAX; ++q) acc[q] = cplx<T>{0, 0};
+      for (int r = 0; r < RB; ++r)
+#pragma unroll
+        for (int q = 0; q < QMAX; ++q) acc[r][q] = cplx<T>{0, 0};
       for (int k0 = 0; k0 < K; k0 += smrows) {
         const int kc = min(smrows, K - k0);
         if (!whole) fill(k0, kc);
-        if (g < n) {
-          for (int kk = 0; kk < kc; ++kk) {
-            const cplx<T> w = W[(size_t)(k0 + kk) * npwx + g];
-            const cplx<T>* ck = smbuf + (size_t)kk * P + s0 + sg;
+        for (int kk = 0; kk < kc; ++kk) {
+          cplx<T> w[RB];
 #pragma unroll
-            for (int q = 0; q < QMAX; ++q)
-              if (s0 + sg + q * sgrp < ns) cfma(acc[q], w, ck[q * sgrp]);
+          for (int r = 0; r < RB; ++r) {
+            const int g = g0 + gl + r * GR;
+            w[r] = g < n ? W[(size_t)(k0 + kk) * npwx + g] : cplx<T>{0, 0};
+          }
+          const cplx<T>* ck = smbuf + (size_t)kk * P + s0 + sg;
+#pragma unroll
+          for (int q = 0; q < QMAX; ++q) {
+            if (s0 + sg + q * sgrp < ns) {
+              const cplx<T> c = ck[q * sgrp];
+#pragma unroll
+              for (int r = 0; r < RB; ++r) cfma(acc[r][q], w[r], c);
+            }
           }
         }
       }
-      if (g < n) {
 #pragma unroll
-        for (int q = 0; q < QMAX; ++q) {
-          const int s = s0 + sg + q * sgrp;
-          if (s < ns) {
-            cplx<T> v = acc[q];
-            if (Z) v += ccast<T>(carry[s]) * Z[(size_t)s * npwx + g];
-            cplx<T>* dst = y + (size_t)s * ldy + g;
-            *dst = accumulate ? *dst + v : v;
+      for (int r = 0; r < RB; ++r) {
+        const int g = g0 + gl + r * GR;
+        if (g < n) {
+#pragma unroll
+          for (int q = 0; q < QMAX; ++q) {
+            const int s = s0 + sg + q * sgrp;
+            if (s < ns) {
+              cplx<T> v = acc[r][q];
+              if (Z) v += ccast<T>(carry[s]) * Z[(size_t)s * npwx + g];
+              cplx<T>* dst = y + (size_t)s * ldy + g;
+              *dst = accumulate ? *dst + v : v;
+            }
           }
         }
       }
@@ -683,7 +707,7 @@ __device__ void solve_one(const SolverArgs<T>& a, const ApplyT& A, int rhs, int 
 }
 
 template <typename T, class ApplyT, int THREADS>
-__global__ void __launch_bounds__(THREADS, 1) msbicg_kernel(SolverArgs<T> a, ApplyT A) {
+__global__ void __launch_bounds__(THREADS, CtasPerSm<T>::v) msbicg_kernel(SolverArgs<T> a, ApplyT A) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ SeedShared ss;
   __shared__ int s_rhs;

@@ -70,7 +70,7 @@ __device__ __forceinline__ unsigned long long gtimer() {
 __global__ void stamp_kernel(unsigned long long* t) { *t = gtimer(); }
 
 template <typename T, class ApplyT, int THREADS>
-__global__ void __launch_bounds__(THREADS, 1)
+__global__ void __launch_bounds__(THREADS, CtasPerSm<T>::v)
     msbicg_multi_kernel(const MultiItem* items, int nitems, int* counter, cplx<T>* col_global, long long col_slot,
                         unsigned long long* sys_end) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -377,7 +377,7 @@ sgw_status launch_solve_stage(sgw_multi* P, std::vector<MultiGroup>& groups, int
     SGW_CK(cudaMemsetAsync(counter, 0, sizeof(int), P->stream));
     SGW_CK(cudaMemcpyToSymbolAsync(c_entries, g.entries.p, g.entry_bytes, 0, cudaMemcpyDeviceToDevice, P->stream));
     constexpr int NT = CtaThreads<T>::v;
-    const int grid = std::max(1, std::min(P->nslots, g.nitems));
+    const int grid = std::max(1, std::min(P->num_sms * CtasPerSm<T>::v, g.nitems));
     unsigned long long* sys_end = P->stamps.as<unsigned long long>() + 1;
     long long col_slot = 0;
     for (int i = 0; i < P->nsys; ++i)
@@ -403,7 +403,7 @@ sgw_status launch_res_stage(sgw_multi* P, int& counter_idx) {
     SGW_CK(cudaMemsetAsync(counter, 0, sizeof(int), P->stream));
     SGW_CK(cudaMemcpyToSymbolAsync(c_entries, g.entries.p, g.entry_bytes, 0, cudaMemcpyDeviceToDevice, P->stream));
     constexpr int NT = CtaThreads<double>::v;
-    const int grid = std::max(1, std::min(P->nslots, g.nitems));
+    const int grid = std::max(1, std::min(P->num_sms, g.nitems));
     unsigned long long* sys_end = P->stamps.as<unsigned long long>() + 1;
     long long col_slot = 0;
     for (int i = 0; i < P->nsys; ++i)
@@ -538,7 +538,7 @@ sgw_status multi_create(int nsys, sgw_operator* const* ops, const sgw_batch_desc
   P->d.assign(descs, descs + nsys);
   P->opt = o;
   P->num_sms = ops[0]->num_sms;
-  P->nslots = P->num_sms;
+  P->nslots = P->num_sms * std::max(CtasPerSm<float>::v, CtasPerSm<double>::v);
   auto fail = [&](sgw_status s) {
     sgw_multi_destroy(P);
     return s;
@@ -707,7 +707,8 @@ template <typename T>
 std::vector<PwShape> tune_candidates(sgw_operator* op) {
   const PwView<T>& v = pwview<T>(op);
   const size_t static_bytes = sizeof(SeedShared) + 64;
-  const size_t budget = op->smem_optin > static_bytes ? op->smem_optin - static_bytes : 0;
+  const size_t per_cta = std::min(op->smem_optin, op->smem_per_sm / CtasPerSm<T>::v - 1024);
+  const size_t budget = per_cta > static_bytes ? per_cta - static_bytes : 0;
   const size_t colb = (size_t)v.ncol * v.ldz * sizeof(cplx<T>);
   auto small = [&](int ng) { return (size_t)pw_smem_small(v, ng) * sizeof(cplx<T>); };
   std::vector<PwShape> c;
@@ -761,7 +762,7 @@ sgw_status tune(sgw_operator* op, sgw_tune_result* res) {
     set_error("no FFT launch shape fits in shared memory");
     return SGW_ERR_UNSUPPORTED;
   }
-  const int m = 2 * op->num_sms;
+  const int m = 2 * op->num_sms * CtasPerSm<T>::v;
   const int npwx = op->npwx;
   DevBuf x, y;
   sgw_status s;
@@ -788,7 +789,7 @@ sgw_status tune(sgw_operator* op, sgw_tune_result* res) {
       SGW_CK(cudaEventElapsedTime(&t, op->lev0, op->lev1));
       if (rep > 0) tmin = std::min(tmin, t);
     }
-    const double us = 1e3 * tmin * op->num_sms / (double)m;  // one apply on one CTA
+    const double us = 1e3 * tmin * op->num_sms * CtasPerSm<T>::v / (double)m;  // one apply on one CTA
     if (us < best) {
       best = us;
       best_s = c;

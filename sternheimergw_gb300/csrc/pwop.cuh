@@ -33,6 +33,9 @@ struct PwView {
   const int* g_i3;     // [npw] i3 of each sphere point
   const int* col_pos;  // [ncol] i1 + pitch * i2
   const int* i1_list;  // [ni1] i1 values holding columns
+  const unsigned long long* ymask;  // [ni1] bit i2 set where column (i1_list[l], i2) exists
+  const unsigned long long* zmask;  // [ncol] bit i3 set where the column holds a sphere point
+  unsigned long long xmask;         // bit i1 set for every i1 in i1_list
   const T* g2kin;      // [npw]
   const T* vrs;        // [nnr] V_loc(r), index i1 + nr1 (i2 + nr2 i3)
   int nkb;
@@ -46,9 +49,16 @@ struct PwView {
 };
 
 // Shared-memory elements (cplx<T>) the apply needs besides the column store.
+// Shared-memory elements (cplx<T> units) holding the column positions col_pos.
+template <typename T>
+__host__ __device__ inline int pw_cpos_units(const PwView<T>& op) {
+  constexpr int per = (int)(sizeof(cplx<T>) / sizeof(int));
+  return (op.ncol + per - 1) / per;
+}
+
 template <typename T>
 __host__ __device__ inline int pw_smem_small(const PwView<T>& op, int ng) {
-  return op.nr1 + op.nr2 + op.nr3 + op.nkb + op.nocc + ng * op.nr2 * op.pitch;
+  return op.nr1 + op.nr2 + op.nr3 + op.nkb + op.nocc + pw_cpos_units(op) + ng * op.nr2 * op.pitch;
 }
 
 // CTA-wide sum of a double2 partial; result broadcast to every thread.
@@ -96,7 +106,7 @@ __device__ void pw_apply_cta(const PwView<T>& op, const int NG, const cplx<T>* _
   const cplx<T>* tw2 = sm + op.nr1;
   const cplx<T>* tw3 = sm + op.nr1 + op.nr2;
   cplx<T>* bec = sm + op.nr1 + op.nr2 + op.nr3;
-  cplx<T>* planes = bec + op.nkb + op.nocc;
+  cplx<T>* planes = bec + op.nkb + op.nocc + pw_cpos_units(op);
   const int nocc = (op.alpha_pv > 1e-14 || op.alpha_pv < -1e-14) ? op.nocc : 0;  // eps14, linear_op.f90:131
 
   // <beta_i|psi> D_i and alpha_pv <evq_v|psi>, one warp per projection
@@ -174,13 +184,18 @@ __device__ void pw_apply_cta_lines(const PwView<T>& op, const int PF, const cplx
   const cplx<T>* tw2 = sm + op.nr1;
   const cplx<T>* tw3 = sm + op.nr1 + op.nr2;
   cplx<T>* bec = sm + op.nr1 + op.nr2 + op.nr3;
-  cplx<T>* planes = bec + op.nkb + op.nocc;
+  int* cpos = reinterpret_cast<int*>(bec + op.nkb + op.nocc);
+  cplx<T>* planes = bec + op.nkb + op.nocc + pw_cpos_units(op);
   const int nocc = (op.alpha_pv > 1e-14 || op.alpha_pv < -1e-14) ? op.nocc : 0;  // eps14, linear_op.f90:131
   const int ldz = op.ldz, pitch = op.pitch, psz = op.nr2 * op.pitch;
 
+  // <beta_i|psi> D_i and alpha_pv <evq_v|psi>, one warp per projection; the
+  // unrolled loop keeps eight loads of each lane in flight (the projectors
+  // stream from L2)
   for (int i = warp; i < op.nkb + nocc; i += nwarp) {
     const cplx<T>* pr = (i < op.nkb) ? op.vkb + (size_t)i * op.npwx : op.evq + (size_t)(i - op.nkb) * op.npwx;
     cplx<T> acc = {0, 0};
+#pragma unroll 8
     for (int g = lane; g < op.npw; g += 32) cfma_conj(acc, pr[g], in[g]);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
@@ -189,8 +204,10 @@ __device__ void pw_apply_cta_lines(const PwView<T>& op, const int PF, const cplx
     }
     if (lane == 0) bec[i] = (i < op.nkb ? op.dvan[i] : (T)op.alpha_pv) * acc;
   }
-  for (int e = tid; e < op.ncol * ldz; e += nt) col[e] = cplx<T>{0, 0};
-  __syncthreads();
+  for (int c = tid; c < op.ncol; c += nt) cpos[c] = op.col_pos[c];
+  // the column store is not cleared: the inverse i3 pass reads only the
+  // points that hold sphere values (zmask), and every later reader reads
+  // points written earlier in the same apply
   for (int g = tid; g < op.npw; g += nt) col[op.g_col[g] * ldz + op.g_i3[g]] = in[g];
   __syncthreads();
 
@@ -210,13 +227,22 @@ __device__ void pw_apply_cta_lines(const PwView<T>& op, const int PF, const cplx
       if (c < 0) continue;
       cplx<T> v[N];
       cplx<T>* line = col + c * ldz;
+      if constexpr (S > 0) {
+        const unsigned long long m = op.zmask[c];
 #pragma unroll
-      for (int i = 0; i < N; ++i) v[i] = line[i];
+        for (int i = 0; i < N; ++i) v[i] = ((m >> i) & 1ull) ? line[i] : cplx<T>{0, 0};
+      } else {
+#pragma unroll
+        for (int i = 0; i < N; ++i) v[i] = line[i];
+      }
       fft_reg<T, N, S>(v, tw3);
 #pragma unroll
       for (int i = 0; i < N; ++i) line[i] = v[i];
     }
   };
+  // The inverse i2 pass reads only the (i1, i2) points that hold a column
+  // (ymask) and treats the rest as zero, so planes are never cleared; every
+  // later pass reads points written earlier in the same round.
   auto ypass = [&](auto NN, auto SS, int np) {
     constexpr int N = decltype(NN)::value, S = decltype(SS)::value;
     for (int rd = 0, nr = rounds_of(np * op.ni1); rd < nr; ++rd) {
@@ -225,8 +251,14 @@ __device__ void pw_apply_cta_lines(const PwView<T>& op, const int PF, const cplx
       const int p = e / op.ni1, l = e - p * op.ni1;
       cplx<T>* line = planes + p * psz + op.i1_list[l];
       cplx<T> v[N];
+      if constexpr (S > 0) {
+        const unsigned long long m = op.ymask[l];
 #pragma unroll
-      for (int i = 0; i < N; ++i) v[i] = line[i * pitch];
+        for (int i = 0; i < N; ++i) v[i] = ((m >> i) & 1ull) ? line[i * pitch] : cplx<T>{0, 0};
+      } else {
+#pragma unroll
+        for (int i = 0; i < N; ++i) v[i] = line[i * pitch];
+      }
       fft_reg<T, N, S>(v, tw2);
 #pragma unroll
       for (int i = 0; i < N; ++i) line[i * pitch] = v[i];
@@ -239,11 +271,9 @@ __device__ void pw_apply_cta_lines(const PwView<T>& op, const int PF, const cplx
   __syncthreads();
   for (int p0 = 0; p0 < op.nr3; p0 += PF) {
     const int np = min(PF, op.nr3 - p0);
-    for (int e = tid; e < np * psz; e += nt) planes[e] = cplx<T>{0, 0};
-    __syncthreads();
     for (int e = tid; e < np * op.ncol; e += nt) {
       const int p = e / op.ncol, c = e - p * op.ncol;
-      planes[p * psz + op.col_pos[c]] = col[c * ldz + p0 + p];
+      planes[p * psz + cpos[c]] = col[c * ldz + p0 + p];
     }
     __syncthreads();
     with_len<T>(op.nr2, [&](auto NN) { ypass(NN, PLUS{}, np); });
@@ -257,8 +287,9 @@ __device__ void pw_apply_cta_lines(const PwView<T>& op, const int PF, const cplx
         cplx<T>* row = planes + p * psz + i2 * pitch;
         const T* vr = op.vrs + ((size_t)(p0 + p) * op.nr2 + i2) * op.nr1;
         cplx<T> v[N];
+        const unsigned long long xm = op.xmask;
 #pragma unroll
-        for (int i = 0; i < N; ++i) v[i] = row[i];
+        for (int i = 0; i < N; ++i) v[i] = ((xm >> i) & 1ull) ? row[i] : cplx<T>{0, 0};
         fft_reg<T, N, 1>(v, tw1);
 #pragma unroll
         for (int i = 0; i < N; ++i) v[i] = vr[i] * v[i];
@@ -272,7 +303,7 @@ __device__ void pw_apply_cta_lines(const PwView<T>& op, const int PF, const cplx
     __syncthreads();
     for (int e = tid; e < np * op.ncol; e += nt) {
       const int p = e / op.ncol, c = e - p * op.ncol;
-      col[c * ldz + p0 + p] = planes[p * psz + op.col_pos[c]];
+      col[c * ldz + p0 + p] = planes[p * psz + cpos[c]];
     }
     __syncthreads();
   }
@@ -284,7 +315,9 @@ __device__ void pw_apply_cta_lines(const PwView<T>& op, const int PF, const cplx
   for (int g = tid; g < op.npw; g += nt) {
     const cplx<T> x = in[g];
     cplx<T> r = op.g2kin[g] * x + sg * x + scale * col[op.g_col[g] * ldz + op.g_i3[g]];
+#pragma unroll 8
     for (int i = 0; i < op.nkb; ++i) cfma(r, op.vkb[(size_t)i * op.npwx + g], bec[i]);
+#pragma unroll 8
     for (int v = 0; v < nocc; ++v) cfma(r, op.evq[(size_t)v * op.npwx + g], bec[op.nkb + v]);
     out[g] = r;
     if (out2) out2[g] = r;

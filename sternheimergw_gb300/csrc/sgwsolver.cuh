@@ -129,7 +129,7 @@ __global__ void __launch_bounds__(THREADS, 1) sgw_solver_kernel(SgwArgs<T> a, Ap
 
 // One CTA per vector: ax_i = A(sigma) x_i (the reference's AA callback).
 template <typename T, class ApplyT, int THREADS>
-__global__ void __launch_bounds__(THREADS, 1) apply_kernel(ApplyT A, int m, const cplx<T>* x, long long ldi, cplx<T>* ax,
+__global__ void __launch_bounds__(THREADS, CtasPerSm<T>::v) apply_kernel(ApplyT A, int m, const cplx<T>* x, long long ldi, cplx<T>* ax,
                                                             long long ldo, zcd sigma, cplx<T>* col_global,
                                                             long long col_slot) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
