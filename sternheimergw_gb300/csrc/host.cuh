@@ -78,6 +78,7 @@ struct BatchDev {
   int* iters;
   const int* active;  // optional: 0 skips a right-hand side
   zcd* zeta;          // optional: per-shift residual factors at exit
+  int gemm_tc = 0;     // FP32: basis product on the tensor cores (3xTF32)
 };
 
 struct Workspace {

@@ -82,6 +82,7 @@ sgw_status run_msbicg(sgw_operator* op, const BatchDev& b) {
   a.mode = mode;
   a.active = b.active;
   a.zeta = b.zeta;
+  a.gemm_tc = b.gemm_tc;
   return with_applier<T>(op, [&](auto A, size_t smem) -> sgw_status {
     constexpr int NT = CtaThreads<T>::v;
     auto kern = msbicg_kernel<T, decltype(A), NT>;

@@ -60,7 +60,6 @@ sgw_status solve_mixed(sgw_operator* op, const BatchDev& b, int refine_max, doub
   // round 0 right-hand side: b itself
   SGW_CK(cudaMemcpy2DAsync(r64, sizeof(zcd) * npwx, bb, sizeof(zcd) * b.ldb, sizeof(zcd) * n, R,
                            cudaMemcpyDeviceToDevice, op->stream));
-  int rounds_done = 0;
   bool all_done = false;
   for (int round = 0; round <= refine_max; ++round) {
     SGW_CK(cudaMemsetAsync(nactive, 0, sizeof(int), op->stream));
@@ -75,8 +74,11 @@ sgw_status solve_mixed(sgw_operator* op, const BatchDev& b, int refine_max, doub
       break;
     }
     if (round == refine_max) break;
+    // the correction rounds run the basis product on the tensor cores (3xTF32): their
+    // solutions are scaled by |r| / |b| ~ 1e-5, so its ~4x larger rounding than
+    // FP32 FMAs stays far below the refinement target
     BatchDev bf{R, S, b.lmax, b.max_iter, b.history_iters, kRoundRelThreshold, r32, npwx, b.sigma, b.lds, y32,
-                npwx, (long long)S * npwx, b.ierr, iters_round, active, zeta};
+                npwx, (long long)S * npwx, b.ierr, iters_round, active, zeta, round > 0 ? 1 : 0};
     if ((s = run_msbicg<float>(op, bf)) != SGW_OK) return s;
     mx_accumulate<<<std::min(4096, (int)(((long long)R * S * n + tb - 1) / tb)), tb, 0, op->stream>>>(
         R, S, n, npwx, y32, x, b.ldx, b.ldr, Z, scale, active, round == 0);
@@ -101,9 +103,7 @@ sgw_status solve_mixed(sgw_operator* op, const BatchDev& b, int refine_max, doub
       return SGW_OK;
     });
     if (s != SGW_OK) return s;
-    rounds_done = round + 1;
   }
-  (void)rounds_done;
   mx_finish<<<R, tb, 0, op->stream>>>(R, S, n, x, b.ldx, b.ldr, active, b.ierr, all_done ? 0 : 1);
   op->last_launches += 1;
   SGW_CK(cudaGetLastError());

@@ -65,6 +65,7 @@ struct SolverArgs {
   cplx<T>* col_global; // [slot][ncol*ldz] when the column store does not fit in shared memory
   long long col_slot;
   int mode;            // 0 coefficient-space shifts, 1 explicit shift vectors
+  int gemm_tc;         // FP32: 1 runs the basis product on the tensor cores (3xTF32)
   const int* active;   // optional [rhs]: 0 skips the right-hand side
   zcd* zeta;           // optional [rhs][nshift]: residual factor 1/(theta phi) of each shift at exit
 };
@@ -320,6 +321,122 @@ struct GemmShape {
   static constexpr int QMAX = sizeof(T) == 4 ? 18 : 8;  // shifts per thread per pass
 };
 
+// ---------------------------------------------------------------------------
+// FP32 basis product on the tensor cores, 3xTF32 (split products accumulated
+// in FP32): a = a_hi + a_lo with a_hi = tf32(a), a_lo = tf32(a - a_hi), and
+// a b ~ a_hi b_hi + a_hi b_lo + a_lo b_hi, which keeps FP32-level accuracy.
+// The complex product is one real product over an interleaved K' = 2K:
+//   A[g][2k + j]  = (Re, Im)[j] of W[k][g]
+//   Br[2k + j][s] = (Re C[k][s], -Im C[k][s])[j]   ->  Re y = A Br
+//   Bi[2k + j][s] = (Im C[k][s],  Re C[k][s])[j]   ->  Im y = A Bi
+// Warps take 16-row tiles of y; each holds all shift tiles (8 wide) of its
+// row tile in registers.  mma.sync m16n8k8 fragment layout (PTX ISA, tf32):
+// A a0..a3 = (grp, tg), (grp+8, tg), (grp, tg+4), (grp+8, tg+4);
+// B b0, b1 = (tg, grp), (tg+4, grp); D d0..d3 = (grp, 2tg), (grp, 2tg+1),
+// (grp+8, 2tg), (grp+8, 2tg+1); grp = lane / 4, tg = lane % 4.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ unsigned tf32_of(float x) {
+  unsigned r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+  return r;
+}
+
+__device__ __forceinline__ void split_tf32(float x, unsigned& hi, unsigned& lo) {
+  hi = tf32_of(x);
+  lo = tf32_of(x - __uint_as_float(hi));
+}
+
+__device__ __forceinline__ void mma_tf32(float (&d)[4], const unsigned (&a)[4], unsigned b0, unsigned b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "{%0,%1,%2,%3};"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+constexpr int kTcMaxShiftTiles = 12;  // shifts per pass: 96
+
+// y[s][g] (+)= sum_{k < kc} W[k][g] Cs[k][s] (+ carry[s] Z[s][g]); Cs = smem rows [kc][P]
+__device__ inline void tc_basis_gemm_chunk(zcf* y, long long ldy, bool accumulate, const zcf* W, int kc,
+                                           const zcf* Cs, int P, const zcd* carry, const zcf* Z, int ns, int n,
+                                           int npwx) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+  const int grp = lane >> 2, tg = lane & 3;
+  const int kp = 2 * kc;                       // real K'
+  const int ksteps = (kp + 7) / 8;
+  for (int s0 = 0; s0 < ns; s0 += 8 * kTcMaxShiftTiles) {
+    const int ntile = min(kTcMaxShiftTiles, (ns - s0 + 7) / 8);
+    for (int g0 = warp * 16; g0 < n; g0 += nwarp * 16) {
+      float dr[kTcMaxShiftTiles][4], di[kTcMaxShiftTiles][4];
+#pragma unroll
+      for (int t = 0; t < kTcMaxShiftTiles; ++t)
+#pragma unroll
+        for (int e = 0; e < 4; ++e) dr[t][e] = di[t][e] = 0.f;
+      const int ga = g0 + grp, gb = g0 + grp + 8;
+      for (int st = 0; st < ksteps; ++st) {
+        // A fragment: columns k' = 8 st + tg and 8 st + tg + 4 -> complex k = 4 st + tg/2 (+2), part tg%2
+        unsigned ah[4], al[4];
+        {
+          const int k1 = 4 * st + (tg >> 1), k2 = k1 + 2;
+          const int part = tg & 1;
+          auto wval = [&](int k, int g) -> float {
+            if (k >= kc || g >= n) return 0.f;
+            const zcf w = W[(size_t)k * npwx + g];
+            return part ? w.im : w.re;
+          };
+          split_tf32(wval(k1, ga), ah[0], al[0]);
+          split_tf32(wval(k1, gb), ah[1], al[1]);
+          split_tf32(wval(k2, ga), ah[2], al[2]);
+          split_tf32(wval(k2, gb), ah[3], al[3]);
+        }
+        // B rows k' = 8 st + tg (b0) and 8 st + tg + 4 (b1), same complex k pattern as A
+        const int kb1 = 4 * st + (tg >> 1), kb2 = kb1 + 2;
+        const int part = tg & 1;
+#pragma unroll
+        for (int t = 0; t < kTcMaxShiftTiles; ++t) {
+          if (t < ntile) {
+            const int sc = s0 + 8 * t + grp;
+            const bool ok = sc < ns;
+            const zcf c1 = (ok && kb1 < kc) ? Cs[(size_t)kb1 * P + sc] : zcf{0.f, 0.f};
+            const zcf c2 = (ok && kb2 < kc) ? Cs[(size_t)kb2 * P + sc] : zcf{0.f, 0.f};
+            // Br: (Re, -Im)[part]; Bi: (Im, Re)[part]
+            const float r1 = part ? -c1.im : c1.re, r2 = part ? -c2.im : c2.re;
+            const float i1 = part ? c1.re : c1.im, i2 = part ? c2.re : c2.im;
+            unsigned rh1, rl1, rh2, rl2, ih1, il1, ih2, il2;
+            split_tf32(r1, rh1, rl1);
+            split_tf32(r2, rh2, rl2);
+            split_tf32(i1, ih1, il1);
+            split_tf32(i2, ih2, il2);
+            mma_tf32(dr[t], al, rh1, rh2);
+            mma_tf32(dr[t], ah, rl1, rl2);
+            mma_tf32(dr[t], ah, rh1, rh2);
+            mma_tf32(di[t], al, ih1, ih2);
+            mma_tf32(di[t], ah, il1, il2);
+            mma_tf32(di[t], ah, ih1, ih2);
+          }
+        }
+      }
+      // D: (grp, 2tg), (grp, 2tg+1), (grp+8, 2tg), (grp+8, 2tg+1)
+#pragma unroll
+      for (int t = 0; t < kTcMaxShiftTiles; ++t) {
+        if (t < ntile) {
+#pragma unroll
+          for (int e = 0; e < 4; ++e) {
+            const int g = g0 + grp + (e >= 2 ? 8 : 0);
+            const int sidx = s0 + 8 * t + 2 * tg + (e & 1);
+            if (g < n && sidx < ns) {
+              zcf v = {dr[t][e], di[t][e]};
+              if (Z) v += ccast<float>(carry[sidx]) * Z[(size_t)sidx * npwx + g];
+              zcf* dst = y + (size_t)sidx * ldy + g;
+              *dst = accumulate ? *dst + v : v;
+            }
+          }
+        }
+      }
+    }
+  }
+}
+
 // y[s][g] (+)= sum_k W[k][g] C[k][s] (+ carry[s] Z[s][g]) for g < n, s < ns.
 // Threads form (GL/RB) row lanes x (blockDim*RB/GL) shift groups; each thread
 // keeps RB rows x QMAX shifts of accumulators, so every coefficient read from
@@ -327,7 +444,7 @@ struct GemmShape {
 template <typename T>
 __device__ void cta_basis_gemm(cplx<T>* y, long long ldy, bool accumulate, const cplx<T>* W, int K, const zcd* C,
                                int P, const zcd* carry, const cplx<T>* Z, int ns, int n, int npwx, zcd* cvt,
-                               cplx<T>* smbuf, int smrows) {
+                               cplx<T>* smbuf, int smrows, bool tc = false) {
   constexpr int GL = GemmShape<T>::GL, RB = GemmShape<T>::RB, QMAX = GemmShape<T>::QMAX;
   constexpr int GR = GL / RB;  // row lanes
   const cplx<T>* Ck;
@@ -338,6 +455,19 @@ __device__ void cta_basis_gemm(cplx<T>* y, long long ldy, bool accumulate, const
     for (long long e = threadIdx.x; e < (long long)K * P; e += blockDim.x) c32[e] = ccast<T>(C[e]);
     __syncthreads();
     Ck = c32;
+    // tensor cores (3xTF32), coefficients staged in shared memory chunk by chunk
+    for (int k0 = 0; tc && k0 < K; k0 += smrows) {
+      const int kc = min(smrows, K - k0);
+      __syncthreads();
+      for (int e = threadIdx.x; e < kc * P; e += blockDim.x) smbuf[e] = Ck[(size_t)k0 * P + e];
+      __syncthreads();
+      tc_basis_gemm_chunk(y, ldy, accumulate || k0 > 0, W + (size_t)k0 * npwx, kc, smbuf, P, carry,
+                          k0 == 0 ? Z : nullptr, ns, n, npwx);
+    }
+    if (tc) {
+      __syncthreads();
+      return;
+    }
   }
   const int sgrp = blockDim.x / GR;
   const int gl = threadIdx.x % GR, sg = threadIdx.x / GR;
@@ -486,9 +616,9 @@ __device__ void solve_one(const SolverArgs<T>& a, const ApplyT& A, int rhs, int 
     if (track && kw + Db > a.Kcap) {
       // materialise x^sigma and u_0^sigma, start a new window
       cta_basis_gemm<T>(xout + a.ldx, a.ldx, flushed, W, kw, C + L.o_xa, L.P, C + L.o_scal + SC_XD * L.P,
-                        flushed ? U0S : nullptr, Sm1, n, npwx, C + L.o_cvt, gbuf, grows);
+                        flushed ? U0S : nullptr, Sm1, n, npwx, C + L.o_cvt, gbuf, grows, a.gemm_tc);
       cta_basis_gemm<T>(U0S, npwx, false, W, kw, C + L.o_ub, L.P, C + L.o_scal + SC_UC * L.P,
-                        flushed ? U0S : nullptr, Sm1, n, npwx, C + L.o_cvt, gbuf, grows);
+                        flushed ? U0S : nullptr, Sm1, n, npwx, C + L.o_cvt, gbuf, grows, a.gemm_tc);
       __syncthreads();
       for (int s = tid; s < Sm1; s += nt) {  // new window: rows are rewritten before they are read
         const ShiftRef sh{C, s, L.P};
@@ -672,7 +802,7 @@ __device__ void solve_one(const SolverArgs<T>& a, const ApplyT& A, int rhs, int 
   v_copy(xout, X, n);
   if (track)
     cta_basis_gemm<T>(xout + a.ldx, a.ldx, flushed, W, kw, C + L.o_xa, L.P, C + L.o_scal + SC_XD * L.P,
-                      flushed ? U0S : nullptr, Sm1, n, npwx, C + L.o_cvt, gbuf, grows);
+                      flushed ? U0S : nullptr, Sm1, n, npwx, C + L.o_cvt, gbuf, grows, a.gemm_tc);
   if (explicit_mode)
     for (long long e = tid; e < (long long)Sm1 * n; e += nt) {
       const int s = (int)(e / n), g = (int)(e - (long long)s * n);
@@ -686,7 +816,9 @@ __device__ void solve_one(const SolverArgs<T>& a, const ApplyT& A, int rhs, int 
   __syncthreads();
   if (tid == 0) ss.flag = 0;
   __syncthreads();
-  for (int e = tid; e < S * n; e += nt) {
+  // NaN scan of the outputs (bicgstab.f90:264-267); a mixed-precision round
+  // (zeta exported) skips it: the refinement driver scans the FP64 result
+  for (int e = tid; !a.zeta && e < S * n; e += nt) {
     const int s = e / n, g = e - s * n;
     const cplx<T> v = xout[(size_t)s * a.ldx + g];
     if (v.re != v.re || v.im != v.im) ss.flag = 1;

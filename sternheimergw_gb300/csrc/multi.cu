@@ -149,6 +149,7 @@ std::mutex g_const_mutex;  // c_entries is one per process: runs never overlap
 struct MultiGroup {
   bool lines = false;
   DevBuf entries;  // device copy of the constant-memory image
+  DevBuf entries_tc;  // FP32 correction rounds: the same image with the tensor-core basis product
   size_t entry_bytes = 0;
   DevBuf items;
   int nitems = 0;
@@ -303,7 +304,10 @@ sgw_status build_solve_groups(sgw_multi* P, std::vector<MultiGroup>& groups, Dev
         g.smem = std::max(g.smem, sh.smem);
       }
       g.entry_bytes = sizeof(E) * ns;
-      return g.entries.upload(reinterpret_cast<unsigned char*>(img.data()), g.entry_bytes);
+      sgw_status st = g.entries.upload(reinterpret_cast<unsigned char*>(img.data()), g.entry_bytes);
+      if (st != SGW_OK || sizeof(T) == 8) return st;
+      for (int i : sys) img[i].a.gemm_tc = 1;
+      return g.entries_tc.upload(reinterpret_cast<unsigned char*>(img.data()), g.entry_bytes);
     };
     s = lines ? build(PwA<T, true>{}) : build(PwA<T, false>{});
     if (s != SGW_OK) return s;
@@ -371,11 +375,13 @@ sgw_status build_res_groups(sgw_multi* P) {
 
 // Launch one stage: every group of it (constant image, counter reset, persistent launch).
 template <typename T>
-sgw_status launch_solve_stage(sgw_multi* P, std::vector<MultiGroup>& groups, int& counter_idx, DevBuf& col) {
+sgw_status launch_solve_stage(sgw_multi* P, std::vector<MultiGroup>& groups, int& counter_idx, DevBuf& col,
+                              bool tc = false) {
   for (MultiGroup& g : groups) {
     int* counter = P->counters.as<int>() + counter_idx++;
     SGW_CK(cudaMemsetAsync(counter, 0, sizeof(int), P->stream));
-    SGW_CK(cudaMemcpyToSymbolAsync(c_entries, g.entries.p, g.entry_bytes, 0, cudaMemcpyDeviceToDevice, P->stream));
+    SGW_CK(cudaMemcpyToSymbolAsync(c_entries, (tc ? g.entries_tc : g.entries).p, g.entry_bytes, 0,
+                                   cudaMemcpyDeviceToDevice, P->stream));
     constexpr int NT = CtaThreads<T>::v;
     const int grid = std::max(1, std::min(P->num_sms * CtasPerSm<T>::v, g.nitems));
     unsigned long long* sys_end = P->stamps.as<unsigned long long>() + 1;
@@ -486,7 +492,7 @@ sgw_status enqueue(sgw_multi* P) {
       P->launches += 1;
     }
     if (round == rounds) break;
-    sgw_status s = launch_solve_stage<float>(P, P->solve_groups, ci, P->col);
+    sgw_status s = launch_solve_stage<float>(P, P->solve_groups, ci, P->col, round > 0);
     if (s != SGW_OK) return s;
     for (int i = 0; i < ns; ++i) {
       const sgw_batch_desc& d = P->d[i];
@@ -855,6 +861,7 @@ sgw_status sgw_multi_destroy(sgw_multi* plan) {
   for (auto* gs : {&plan->solve_groups, &plan->res_groups})
     for (auto& g : *gs) {
       g.entries.release();
+      g.entries_tc.release();
       g.items.release();
     }
   for (sgw::DevBuf* b : {&plan->vec, &plan->coef, &plan->col, &plan->col64, &plan->counters, &plan->stamps,
