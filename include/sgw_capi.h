@@ -234,6 +234,36 @@ typedef struct sgw_chi_desc {
 
 sgw_status sgw_chi(sgw_operator* op, const sgw_chi_desc* desc);
 
+/* The Green's function of one k-point (green_function, green.f90:105-226):
+ * for every G' point igp of the correlation mesh with ig = ig_of_gp[igp] != 0,
+ * solve (H - omega) x = -delta_{G, ig} for all omega at once (green.f90:199-207,
+ * operator with alpha_pv = 0: green_operator, :231-291), then copy
+ *   green[(f*num_gp + igp)*ldg + i] = x_igp(omega_f)[map[i]]   if 0 < map[i] < npw
+ *                                   = 0                        otherwise
+ * (green.f90:211-213, the reference's WHERE (map > 0 .AND. map < num_g) kept).
+ * Maps are 1-based like the reference's, 0 = no G vector.  All right-hand
+ * sides go through one batched solve (precision 0 FP64, 1 mixed); the handle's
+ * alpha_pv is set to 0 for the call and restored.  *ierr receives the largest
+ * reference error code of the solves.  memory 0: host arrays; 1: device. */
+typedef struct sgw_green_desc {
+  int32_t num_gp;
+  const int32_t* ig_of_gp;
+  int32_t num_g_corr;
+  const int32_t* map;
+  int32_t num_freq;
+  const sgw_zcomplex* omega;
+  int32_t lmax;
+  int32_t max_iter;
+  double threshold;
+  int32_t precision;
+  sgw_zcomplex* green;
+  int64_t ldg;
+  int32_t* ierr;
+  int32_t memory;
+} sgw_green_desc;
+
+sgw_status sgw_green_function(sgw_operator* op, const sgw_green_desc* desc);
+
 /* Replace the local potential V_loc(r) of a plane-wave operator (nnr values,
  * index i1 + nr1 (i2 + nr2 i3), Ry).  Stands for the caller's update of QE's
  * module array vrs before the solve (h_psi reads it; linear_op.f90:46-144). */

@@ -66,3 +66,28 @@ def chi_matrix(bb, x, freq, weight=1.0):
     """bb: (P, nocc, n); x: (Q, nocc, S, n) -> chi (nfreq, P, Q)."""
     c = -np.einsum("pvn,qvsn->spq", np.conj(bb), x) * weight
     return np.moveaxis(average_pm(np.moveaxis(c, 0, -1), freq), -1, 0)
+
+
+def green_function(ops, npw, ig_of_gp, gmap, omega, threshold=1e-10, lmax=4):
+    """green.f90:105-226 with the oracle solver: for every G' point with
+    ig = ig_of_gp[igp] != 0 (1-based) solve (H - omega) x = -delta_ig for all
+    omega, then green[f, igp, i] = x(omega_f)[gmap[i] - 1] where
+    0 < gmap[i] < npw (the reference's WHERE (map > 0 .AND. map < num_g)).
+    ops: oracle operator with alpha_pv = 0."""
+    from . import oracle as O
+    ig = np.asarray(ig_of_gp)
+    gm = np.asarray(gmap)
+    om = np.atleast_1d(np.asarray(omega, dtype=np.complex128))
+    out = np.zeros((om.size, ig.size, gm.size), dtype=np.complex128)
+    rows = [p for p in range(ig.size) if ig[p] != 0]
+    if not rows:
+        return out, 0
+    bb = np.zeros((len(rows), npw), dtype=np.complex128)
+    for r, p in enumerate(rows):
+        bb[r, ig[p] - 1] = -1.0
+    x, ierr, _ = O.bicgstab_many(ops, bb, np.tile(-om, (len(rows), 1)), lmax=lmax, threshold=threshold)
+    ok = (gm > 0) & (gm < npw)
+    for r, p in enumerate(rows):
+        for f in range(om.size):
+            out[f, p, ok] = x[r, f, gm[ok] - 1]
+    return out, int(ierr.max())

@@ -75,6 +75,13 @@ class TuneResult(C.Structure):
                 ("us_per_apply", C.c_double), ("candidates", C.c_int32), ("cached", C.c_int32)]
 
 
+class GreenDesc(C.Structure):
+    _fields_ = [("num_gp", C.c_int32), ("ig_of_gp", C.c_void_p), ("num_g_corr", C.c_int32), ("map", C.c_void_p),
+                ("num_freq", C.c_int32), ("omega", C.c_void_p), ("lmax", C.c_int32), ("max_iter", C.c_int32),
+                ("threshold", C.c_double), ("precision", C.c_int32), ("green", C.c_void_p), ("ldg", C.c_int64),
+                ("ierr", C.c_void_p), ("memory", C.c_int32)]
+
+
 # (name, restype, argtypes) of every entry point declared in include/sgw_capi.h
 SIGNATURES = [
     ("sgw_operator_create_pw", C.c_int, [C.POINTER(PwOperatorDesc), C.POINTER(C.c_void_p)]),
@@ -93,6 +100,7 @@ SIGNATURES = [
     ("sgw_solve_batch_noalloc", C.c_int, [C.c_void_p, C.POINTER(BatchDesc)]),
     ("sgw_coulomb_rhs", C.c_int, [C.c_void_p, C.POINTER(RhsDesc)]),
     ("sgw_chi", C.c_int, [C.c_void_p, C.POINTER(ChiDesc)]),
+    ("sgw_green_function", C.c_int, [C.c_void_p, C.POINTER(GreenDesc)]),
     ("sgw_operator_set_vloc", C.c_int, [C.c_void_p, C.c_void_p, C.c_int64]),
     ("sgw_solve_adjoint", C.c_int, [C.c_void_p, C.POINTER(AdjointDesc)]),
     ("sgw_vjp", C.c_int, [C.c_void_p, C.POINTER(VjpDesc)]),

@@ -2,6 +2,7 @@
 // sides (dvqpsi_us + orthogonalize, rhs.cuh) and the density response with
 // the +-omega average (chi.cuh).
 #include <algorithm>
+#include <cstdint>
 #include <string>
 #include <vector>
 
@@ -182,6 +183,133 @@ static sgw_status chi(sgw_operator* op, const sgw_chi_desc* d) {
   SGW_CK(cudaEventElapsedTime(&ms, op->lev0, op->lev1));
   op->kernel_ms[K_CHI] = ms;
   op->kernel_launches[K_CHI] = 2;
+  return SGW_OK;
+}
+
+// Green's function right-hand sides -delta_{G, ig} and shifts -omega for every listed G' point.
+__global__ void green_rhs_kernel(int nrhs, int n, const int* ig_of_rhs, zcd* bb, const zcd* omega, int S, zcd* sigma) {
+  const long long tot = (long long)nrhs * n;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < tot; e += (long long)gridDim.x * blockDim.x) {
+    const int r = (int)(e / n), g = (int)(e - (long long)r * n);
+    bb[e] = zcd{g == ig_of_rhs[r] - 1 ? -1.0 : 0.0, 0.0};
+  }
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < (long long)nrhs * S;
+       e += (long long)gridDim.x * blockDim.x)
+    sigma[e] = -omega[e % S];
+}
+
+// green[(f * num_gp + igp) * ldg + i] = x[rhs(igp)][f][map[i] - 1] where 0 < map[i] < n, else 0
+__global__ void green_gather_kernel(int num_gp, int num_g_corr, int S, int n, const int* rhs_of_gp, const int* map,
+                                    const zcd* x, zcd* green, long long ldg) {
+  const long long tot = (long long)S * num_gp * num_g_corr;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < tot; e += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(e % num_g_corr);
+    const long long fg = e / num_g_corr;
+    const int igp = (int)(fg % num_gp), f = (int)(fg / num_gp);
+    const int r = rhs_of_gp[igp], m = map[i];
+    zcd v = {0.0, 0.0};
+    if (r >= 0 && m > 0 && m < n) v = x[((size_t)r * S + f) * n + (m - 1)];
+    green[((size_t)f * num_gp + igp) * ldg + i] = v;
+  }
+}
+
+static sgw_status green_function(sgw_operator* op, const sgw_green_desc* d) {
+  if (!op || !d) return lt_arg_error("null argument");
+  if (op->kind != 1) return lt_arg_error("sgw_green_function needs a plane-wave operator");
+  if (d->num_gp < 0 || d->num_g_corr < 0 || d->num_freq < 1 || d->lmax < 1 || d->lmax > kMaxL - 1 ||
+      d->max_iter < 1 || (d->precision != 0 && d->precision != 1) || d->memory < 0 || d->memory > 1)
+    return lt_arg_error("invalid Green's function description");
+  if (!d->ierr || (d->num_gp > 0 && (!d->ig_of_gp || !d->green)) || (d->num_g_corr > 0 && !d->map) || !d->omega)
+    return lt_arg_error("null Green's function array");
+  if (d->ldg < d->num_g_corr) return lt_arg_error("ldg too small");
+  const int n = op->n, S = d->num_freq, G = d->num_gp, M = d->num_g_corr;
+  // the G' list decides the right-hand sides: read it on the host
+  std::vector<int> ig(G);
+  if (G > 0) {
+    if (d->memory == 1)
+      SGW_CK(cudaMemcpy(ig.data(), d->ig_of_gp, sizeof(int) * G, cudaMemcpyDeviceToHost));
+    else
+      std::copy(d->ig_of_gp, d->ig_of_gp + G, ig.begin());
+  }
+  std::vector<int> rhs_of_gp(G, -1), ig_of_rhs;
+  for (int p = 0; p < G; ++p) {
+    if (ig[p] < 0 || ig[p] > n) return lt_arg_error("ig_of_gp outside 0..npw");
+    if (ig[p] != 0) {
+      rhs_of_gp[p] = (int)ig_of_rhs.size();
+      ig_of_rhs.push_back(ig[p]);
+    }
+  }
+  const int R = (int)ig_of_rhs.size();
+  sgw_status s;
+  DevBuf& bbuf = op->lt_bb;   // bb [R][n], then sigma [R][S], the int tables, omega
+  DevBuf& xbuf = op->lt_xx;   // x [R][S][n]
+  DevBuf& gbuf = op->lt_chi;  // green staging (host memory mode)
+  const size_t bb_b = sizeof(zcd) * (size_t)std::max(R, 1) * n;
+  const size_t sg_b = sizeof(zcd) * (size_t)std::max(R, 1) * S;
+  const size_t tab_b = sizeof(int) * ((size_t)std::max(R, 1) + G + std::max(M, 1)) + sizeof(zcd) * S + 256;
+  if ((s = bbuf.ensure(bb_b + sg_b + tab_b)) != SGW_OK) return s;
+  if ((s = xbuf.ensure(sizeof(zcd) * (size_t)std::max(R, 1) * S * n)) != SGW_OK) return s;
+  if ((s = op->st_ierr.ensure(sizeof(int) * std::max(R, 1))) != SGW_OK) return s;
+  if ((s = op->st_iters.ensure(sizeof(int) * std::max(R, 1))) != SGW_OK) return s;
+  unsigned char* base = reinterpret_cast<unsigned char*>(bbuf.p);
+  zcd* bb = reinterpret_cast<zcd*>(base);
+  zcd* sigma = reinterpret_cast<zcd*>(base + bb_b);
+  int* t_ig = reinterpret_cast<int*>(base + bb_b + sg_b);
+  int* t_rhs = t_ig + std::max(R, 1);
+  int* t_map = t_rhs + G;
+  zcd* t_om = reinterpret_cast<zcd*>(reinterpret_cast<unsigned char*>(t_map + std::max(M, 1)) +
+                                     (16 - (reinterpret_cast<uintptr_t>(t_map + std::max(M, 1)) & 15)) % 16);
+  const double keep_alpha = op->alpha_pv;
+  op->alpha_pv = 0.0;  // green_operator (green.f90:283)
+  struct Restore {
+    sgw_operator* o;
+    double a;
+    ~Restore() { o->alpha_pv = a; }
+  } restore{op, keep_alpha};
+  SGW_CK(cudaEventRecord(op->lev0, op->stream));
+  if (R > 0) SGW_CK(cudaMemcpyAsync(t_ig, ig_of_rhs.data(), sizeof(int) * R, cudaMemcpyHostToDevice, op->stream));
+  if (G > 0) SGW_CK(cudaMemcpyAsync(t_rhs, rhs_of_gp.data(), sizeof(int) * G, cudaMemcpyHostToDevice, op->stream));
+  const cudaMemcpyKind in_kind = d->memory == 1 ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+  if (M > 0) SGW_CK(cudaMemcpyAsync(t_map, d->map, sizeof(int) * M, in_kind, op->stream));
+  SGW_CK(cudaMemcpyAsync(t_om, d->omega, sizeof(zcd) * S, in_kind, op->stream));
+  int worst = 0;
+  if (R > 0) {
+    const int grid = std::min(op->num_sms * 8, (int)std::max<long long>(1, ((long long)R * n + 255) / 256));
+    green_rhs_kernel<<<grid, 256, 0, op->stream>>>(R, n, t_ig, bb, t_om, S, sigma);
+    SGW_CK(cudaGetLastError());
+    BatchDev b{R, S, d->lmax, d->max_iter, 0, d->threshold, bb, n, sigma, S, xbuf.p, n, (long long)S * n,
+               op->st_ierr.as<int>(), op->st_iters.as<int>()};
+    s = d->precision == 0 ? run_msbicg<double>(op, b) : solve_mixed(op, b, 0, 0.0);
+    if (s != SGW_OK) return s;
+    std::vector<int> ierr_h(R);
+    SGW_CK(cudaMemcpyAsync(ierr_h.data(), op->st_ierr.p, sizeof(int) * R, cudaMemcpyDeviceToHost, op->stream));
+    SGW_CK(cudaStreamSynchronize(op->stream));
+    for (int v : ierr_h) worst = std::max(worst, v);
+  }
+  if (G > 0 && M > 0) {
+    zcd* gout;
+    long long ldg = d->ldg;
+    if (d->memory == 1) {
+      gout = reinterpret_cast<zcd*>(d->green);
+    } else {
+      if ((s = gbuf.ensure(sizeof(zcd) * (size_t)S * G * M)) != SGW_OK) return s;
+      gout = gbuf.as<zcd>();
+      ldg = M;
+    }
+    const long long tot = (long long)S * G * M;
+    green_gather_kernel<<<(int)std::min<long long>((tot + 255) / 256, op->num_sms * 16), 256, 0, op->stream>>>(
+        G, M, S, n, t_rhs, t_map, xbuf.as<zcd>(), gout, ldg);
+    SGW_CK(cudaGetLastError());
+    if (d->memory == 0)
+      SGW_CK(cudaMemcpy2DAsync(d->green, sizeof(zcd) * d->ldg, gout, sizeof(zcd) * M, sizeof(zcd) * M,
+                               (size_t)S * G, cudaMemcpyDeviceToHost, op->stream));
+  }
+  SGW_CK(cudaEventRecord(op->lev1, op->stream));
+  SGW_CK(cudaStreamSynchronize(op->stream));
+  if (d->memory == 1)
+    SGW_CK(cudaMemcpy(d->ierr, &worst, sizeof(int), cudaMemcpyHostToDevice));
+  else
+    *d->ierr = worst;
   return SGW_OK;
 }
 
@@ -436,6 +564,15 @@ sgw_status sgw_vjp(sgw_operator* op, const sgw_vjp_desc* desc) {
     return sgw::vjp(op, desc);
   } catch (...) {
     sgw::set_error("host exception in sgw_vjp");
+    return SGW_ERR_NOMEM;
+  }
+}
+
+sgw_status sgw_green_function(sgw_operator* op, const sgw_green_desc* desc) {
+  try {
+    return sgw::green_function(op, desc);
+  } catch (...) {
+    sgw::set_error("host exception in sgw_green_function");
     return SGW_ERR_NOMEM;
   }
 }

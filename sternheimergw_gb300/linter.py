@@ -79,6 +79,35 @@ def chi_matrix(op, bb, xx, nbnd, freq, weight=1.0):
     return np.ascontiguousarray(np.transpose(c, (1, 2, 0)))
 
 
+def green_function(op, ig_of_gp, gmap, omega, *, threshold=1e-10, lmax=4, max_iter=10000, precision=0):
+    """green_function (green.f90:105-226) on the GPU (sgw_green_function).
+
+    ig_of_gp: (num_gp,) 1-based G index at k of each G' point of the correlation
+    mesh, 0 = none (map(fft_map(igp)), green.f90:199); gmap: (num_g_corr,)
+    1-based G index of each correlation point, 0 = none; omega: (num_freq,)
+    frequencies (shifts -omega).  Returns (green[num_freq, num_gp, num_g_corr],
+    ierr) with green(i, igp, f) of the reference at green[f, igp, i].
+    """
+    import ctypes as C
+
+    from . import _capi
+    ig = np.ascontiguousarray(ig_of_gp, dtype=np.int32)
+    gm = np.ascontiguousarray(gmap, dtype=np.int32)
+    om = np.ascontiguousarray(np.atleast_1d(omega), dtype=np.complex128)
+    out = np.zeros((om.size, ig.size, gm.size), dtype=np.complex128)
+    ierr = C.c_int32(0)
+    d = _capi.GreenDesc()
+    d.num_gp, d.ig_of_gp = ig.size, ig.ctypes.data
+    d.num_g_corr, d.map = gm.size, gm.ctypes.data
+    d.num_freq, d.omega = om.size, om.ctypes.data
+    d.lmax, d.max_iter, d.threshold, d.precision = int(lmax), int(max_iter), float(threshold), int(precision)
+    d.green, d.ldg = out.ctypes.data, max(gm.size, 1)
+    d.ierr = C.addressof(ierr)
+    d.memory = 0
+    _capi.check(_capi.lib().sgw_green_function(op.handle, C.byref(d)), "sgw_green_function")
+    return out, ierr.value
+
+
 def green_rhs(npw, ig_list):
     """b = -delta_{G, G'} for each G' index (green.f90:203-204): (len, npw)."""
     b = np.zeros((len(ig_list), npw), dtype=np.complex128)

@@ -6,7 +6,10 @@
     side (two 3-D FFTs in another summation order than numpy's pocketfft);
   * sgw_chi: the +-omega average and the projection on the perturbation set
     (solve_linter.f90:462-497, coulomb.f90:146-151).  FP64; tolerance 1e-12
-    relative (a K = nbnd * npw sum in another order).
+    relative (a K = nbnd * npw sum in another order);
+  * sgw_green_function: green.f90:105-226 (G' list, -delta right-hand sides,
+    shifts -omega, integer-map gather) against the oracle solver, 1e-8
+    relative (both stop at the same absolute seed threshold); mixed within 1e-6.
 """
 import numpy as np
 import pytest
@@ -140,3 +143,41 @@ def test_chi_of_solved_c4(c4):
     bref = np.stack([linter_ref.coulomb_rhs(s, ip) for ip in range(npert)])
     ref = linter_ref.chi_matrix(bref, x.reshape(npert, nocc, sh.shape[1], -1), f)
     assert rel(got, ref) < 1e-11
+
+
+def test_green_function_matches_oracle(c4):
+    """green_function (green.f90:105-226): G' list with skipped points, a
+    correlation map with zeros and with the excluded last G vector (the
+    reference's map < num_g), shifts -omega; GPU vs the oracle solver."""
+    from oracle import oracle as O
+    s, f, op = c4
+    n = op.n
+    rng = np.random.default_rng(21)
+    ig_of_gp = rng.integers(1, n + 1, 24).astype(np.int32)
+    ig_of_gp[[3, 11]] = 0
+    gmap = np.arange(1, 151, dtype=np.int32)
+    gmap[[5, 77]] = 0
+    gmap[140] = n                      # excluded by map < num_g
+    mu = 0.5 * s["et"].max()
+    omega = -linter.green_shifts(mu, f[1:6])           # omega = mu +- i w (freqbins.f90:302-323)
+    alpha = op.alpha_pv
+    got, ierr = linter.green_function(op, ig_of_gp, gmap, omega, threshold=1e-10)
+    assert op.alpha_pv == alpha        # the handle keeps its own alpha_pv
+    ops = O.PlaneWaveOperator(s, alpha_pv=0.0)
+    ref, ierr_ref = linter_ref.green_function(ops, n, ig_of_gp, gmap, omega, threshold=1e-10)
+    assert ierr == ierr_ref == 0
+    assert got.shape == ref.shape == (omega.size, 24, 150)
+    assert np.all(got[:, [3, 11], :] == 0) and np.all(got[:, :, [5, 77, 140]] == 0)
+    assert rel(got, ref) < 1e-8
+
+
+def test_green_function_mixed(c4):
+    s, f, op = c4
+    rng = np.random.default_rng(22)
+    ig_of_gp = rng.integers(1, op.n + 1, 16).astype(np.int32)
+    gmap = np.arange(1, 101, dtype=np.int32)
+    omega = (0.3 + 1j * np.linspace(0.1, 2.0, 6))
+    g64, e64 = linter.green_function(op, ig_of_gp, gmap, omega)
+    gm, em = linter.green_function(op, ig_of_gp, gmap, omega, precision=1)
+    assert e64 == em == 0
+    assert rel(gm, g64) < 1e-6
