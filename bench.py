@@ -36,6 +36,15 @@ sys.path.insert(0, ROOT)
 LMAX = 4
 THRESHOLD = 1e-10
 METRIC = "Sternheimer solves/sec: batched mixed vs plain FP64, same GPU, W err ≤1e-6"
+# DRAM read + write of the solver kernels from one ncu capture each (152 right-hand
+# sides of this workload: one CTA wave), per right-hand side; traffic grows with the
+# number of right-hand sides (per-CTA Krylov slots and the solutions), so a full
+# launch is scaled by its right-hand-side count.
+NCU_DRAM_BYTES_PER_RHS = {
+    "fp32": (119.84e6 + 433.01e6) / 152,   # round 0 of the mixed solve
+    "fp64": (2.570702e9 + 2.865210e9) / 152,
+}
+NCU_SOURCE = {"fp32": "profiles/msbicg_fp32_c1_152rhs.md", "fp64": "profiles/msbicg_fp64_c1_152rhs.md"}
 WORKLOAD = "sc8 a=10.26 25Ry 40^3 npw=2293 nkb=32 nocc=16 npert=113 nfreq=35 (S=70) lmax=4 thr=1e-10"
 
 
@@ -590,12 +599,17 @@ def run_gpu(args, rank, world):
             "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h), "ms_per_step": float(np.median(e2e_ms))},
             "roofline": {"bound": "fp32", "achieved": ach32, "peak": peak32, "unit": "TFLOP/s",
-                         "frac": ach32 / peak32, "traffic": None,
+                         "frac": ach32 / peak32, "traffic": NCU_DRAM_BYTES_PER_RHS["fp32"] * nrhs,
+                         "traffic_unit": "bytes per launch (round 0)",
+                         "traffic_source": NCU_SOURCE["fp32"] + ", scaled from 152 to " + str(nrhs) + " RHS",
                          "kernel": "msbicg_kernel<float> (mixed rounds)",
                          "launches_per_step": k32_n / args.steps, "ms_per_launch": k32_ms / max(k32_n, 1),
                          "peak_source": "in-run cuBLAS SGEMM 8192^3, TF32 off"},
             "roofline_fp64": {"bound": "fp64", "achieved": ach64, "peak": peak64, "unit": "TFLOP/s",
-                              "frac": ach64 / peak64, "traffic": None, "kernel": "msbicg_kernel<double>",
+                              "frac": ach64 / peak64, "traffic": NCU_DRAM_BYTES_PER_RHS["fp64"] * nrhs,
+                              "traffic_unit": "bytes per launch",
+                              "traffic_source": NCU_SOURCE["fp64"] + ", scaled from 152 to " + str(nrhs) + " RHS",
+                              "kernel": "msbicg_kernel<double>",
                               "ms_per_launch": k64_ms / max(k64_n, 1), "flops_per_launch": f64,
                               "peak_source": "in-run cuBLAS DGEMM 8192^3 (MEASURED_PEAKS.json has no FP64 figure)"},
             "caller_kernels": {

@@ -224,3 +224,22 @@ def test_mixed_w_error_c4(gpu_lib):
     WM = linter.w_from_chi(linter.chi_matrix(op, bb, xm, nocc, f), v)
     err = np.linalg.norm(WM - W64, axis=(1, 2)) / np.linalg.norm(W64, axis=(1, 2))
     assert err.max() < 1e-6, err.max()
+
+
+def test_large_host_batch_matches_device(lin_prob):
+    """A large host-memory batch (staged copies in and out inside the call) gives
+    exactly the device-memory answer."""
+    import torch
+    A, b, sigma = lin_prob
+    op = sg.DenseOperator(A)
+    rng = np.random.default_rng(12)
+    R = 1400
+    bb = rng.standard_normal((R, A.shape[0])) + 1j * rng.standard_normal((R, A.shape[0]))
+    bb /= np.linalg.norm(bb, axis=1, keepdims=True)
+    sh = np.tile(sigma[:8], (R, 1))
+    for prec in (0, 1):
+        xh, eh, ih = sg.solve_batch(op, bb, sh, threshold=1e-8, precision=prec)
+        xd, ed, idv = sg.solve_batch(op, torch.from_numpy(bb).cuda(), torch.from_numpy(sh).cuda(), threshold=1e-8,
+                                     precision=prec)
+        assert (eh == ed.cpu().numpy()).all() and (ih == idv.cpu().numpy()).all()
+        assert rel(xh, xd.cpu().numpy()) < 1e-14
