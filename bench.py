@@ -544,8 +544,11 @@ def run_gpu(args, rank, world):
     sg_h = torch.from_numpy(sigma).pin_memory()
     x_h = torch.empty((nrhs, S, n), dtype=torch.complex128).pin_memory()
     e2e_ms = []
-    # one untimed call first: it allocates the library's host-path staging buffers
-    sg.solve_batch(op, bb_h.numpy(), sg_h.numpy(), lmax=LMAX, threshold=THRESHOLD, precision=1, out=x_h.numpy())
+    # untimed calls first: they allocate the library's host-path staging buffers and
+    # touch every page of the pinned output once (the first copy into fresh pinned
+    # pages runs at a fraction of the warm bandwidth on this host)
+    for _ in range(2):
+        sg.solve_batch(op, bb_h.numpy(), sg_h.numpy(), lmax=LMAX, threshold=THRESHOLD, precision=1, out=x_h.numpy())
     for k in range(max(1, min(args.steps, 3))):
         flush_l2(l2)
         torch.cuda.synchronize()
@@ -597,7 +600,10 @@ def run_gpu(args, rank, world):
                                            "only shifts near the seed converge, so W is undefined here; the error "
                                            "of mixed vs FP64 is taken over the converged shifts"},
             "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": int(h2d),
-                    "d2h_bytes_per_step": int(d2h), "ms_per_step": float(np.median(e2e_ms))},
+                    "d2h_bytes_per_step": int(d2h), "ms_per_step": float(np.median(e2e_ms)),
+                    "ms_per_step_all": [float(v) for v in e2e_ms],
+                    "note": "median of the timed calls; the device-to-host copy of 4.6 GB into pinned memory "
+                            "varies between 24 ms and ~200 ms on this host"},
             "roofline": {"bound": "fp32", "achieved": ach32, "peak": peak32, "unit": "TFLOP/s",
                          "frac": ach32 / peak32, "traffic": NCU_DRAM_BYTES_PER_RHS["fp32"] * nrhs,
                          "traffic_unit": "bytes per launch (round 0)",
