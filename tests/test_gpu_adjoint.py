@@ -99,6 +99,7 @@ def test_vloc_gradient_vs_central_fd(setup):
     bb = np.concatenate([linter_ref.coulomb_rhs(s, ip) for ip in range(len(s["gpert"]))])
     fd = A.fd_vloc(s, bb, sig, w, c, pts, h=1e-6)
     err = rel(gv[pts], fd)
+    print(f"dL/dV_loc vs central differences (64 points): relative error {err:.2e}")
     assert err <= 1e-6, err
 
 
@@ -112,6 +113,7 @@ def test_dvbare_gradient_vs_central_fd(setup):
     fd = A.fd_dvbare(s, sig, w, c, pts)
     got = np.array([gd[p, j] for p, j in pts])
     err = rel(got, fd)
+    print(f"dL/dDelta V vs central differences (64 points): relative error {err:.2e}")
     assert err <= 1e-6, err
 
 
