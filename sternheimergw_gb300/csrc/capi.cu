@@ -361,6 +361,10 @@ static sgw_status solve_batch(sgw_operator* op, const sgw_batch_desc* d) {
   if (s != SGW_OK) return s;
   op->last_launches = 0;
   op->kev_used = 0;
+  if (d->nrhs == 0) {
+    op->last_ms = 0.0;
+    return SGW_OK;
+  }
   BatchDev b{d->nrhs, d->num_shift, d->lmax, d->max_iter, d->history_iters, d->threshold, nullptr, 0, nullptr, 0,
              nullptr, 0, 0, nullptr, nullptr};
   const int n = op->n, S = d->num_shift, R = d->nrhs;

@@ -112,3 +112,16 @@ def test_new_register_lengths_apply_parity(systems):
     got = op.apply(-0.2 + 0.3j, v)
     ref = O.apply(O.PlaneWaveOperator(s), -0.2 + 0.3j, v)
     assert rel(got, ref) < 1e-13
+
+
+def test_multi_with_empty_system(systems):
+    """A system with no right-hand sides in the plan (ragged batch)."""
+    import torch
+    s, f, op, bb, sh = systems[1]
+    empty = (op, bb[:0].contiguous(), sh[:0].contiguous())
+    plan = sg.solver.MultiPlan([empty, (op, bb, sh)], precision=1, threshold=1e-10, use_graph=True)
+    total, per = plan.run()
+    x, ierr, _ = sg.solve_batch(op, bb, sh, threshold=1e-10, precision=1)
+    assert plan.x[0].shape[0] == 0 and (plan.ierr[1].cpu().numpy() == ierr.cpu().numpy()).all()
+    assert rel(plan.x[1].cpu().numpy(), x.cpu().numpy()) < 1e-13
+    plan.close()

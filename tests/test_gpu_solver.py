@@ -243,3 +243,28 @@ def test_large_host_batch_matches_device(lin_prob):
                                      precision=prec)
         assert (eh == ed.cpu().numpy()).all() and (ih == idv.cpu().numpy()).all()
         assert rel(xh, xd.cpu().numpy()) < 1e-14
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_batch_edge_cases(c0, precision):
+    """Empty batch, a single shift, a zero right-hand side (solution 0, ierr 0), a NaN
+    right-hand side (ierr 2 for that one only) and max_iter = 1 (ierr 1)."""
+    s, f, op, ops = c0
+    bb = linter_ref.coulomb_rhs(s, 0)
+    sh = linter.coulomb_shifts(s, f)
+    x, ierr, iters = sg.solve_batch(op, bb[:0], sh[:0], threshold=1e-10, precision=precision)
+    assert x.shape == (0, sh.shape[1], op.n) and ierr.size == 0
+    x1, e1, _ = sg.solve_batch(op, bb, sh[:, :1], threshold=1e-10, precision=precision)
+    xo, eo, _ = O.bicgstab_many(ops, bb, sh[:, :1], threshold=1e-10)
+    assert (e1 == 0).all() and (eo == 0).all()
+    for r in range(bb.shape[0]):
+        assert rel(x1[r, 0], xo[r, 0]) < (1e-8 if precision == 0 else 1e-7)
+    b2 = bb.copy()
+    b2[1] = 0.0
+    b2[2, 5] = np.nan
+    x2, e2, _ = sg.solve_batch(op, b2, sh, threshold=1e-10, precision=precision, max_iter=200)
+    assert e2[2] == 2 and e2[0] == 0 and e2[3] == 0
+    if precision == 1:   # the refinement driver treats a zero right-hand side as solved
+        assert e2[1] == 0 and np.abs(x2[1]).max() == 0.0
+    x3, e3, _ = sg.solve_batch(op, bb, sh, threshold=1e-14, precision=0, max_iter=1)
+    assert (e3 == 1).all()
