@@ -38,7 +38,7 @@ sgw_status solve_mixed(sgw_operator* op, const BatchDev& b, int refine_max, doub
   const size_t z_b = sizeof(zcd) * (size_t)R * S;
   if ((s = m1.ensure(r64_b + r32_b)) != SGW_OK) return s;
   if ((s = m2.ensure(y32_b)) != SGW_OK) return s;
-  if ((s = m3.ensure(2 * z_b + 2 * sizeof(double) * R + 3 * sizeof(int) * R + 256)) != SGW_OK) return s;
+  if ((s = m3.ensure(2 * z_b + 2 * sizeof(double) * R + 4 * sizeof(int) * R + 256)) != SGW_OK) return s;
   zcd* r64 = m1.as<zcd>();
   zcf* r32 = reinterpret_cast<zcf*>(reinterpret_cast<unsigned char*>(m1.p) + r64_b);
   zcf* y32 = m2.as<zcf>();
@@ -50,11 +50,12 @@ sgw_status solve_mixed(sgw_operator* op, const BatchDev& b, int refine_max, doub
   int* active = reinterpret_cast<int*>(bnorm + R);
   int* iters_round = active + R;
   int* nactive = iters_round + R;
+  int* bad = nactive + R;
   int* iters_total = b.iters;
   const zcd* bb = reinterpret_cast<const zcd*>(b.bb);
   zcd* x = reinterpret_cast<zcd*>(b.xx);
   const int tb = 256;
-  mx_init<<<(R * S + tb - 1) / tb, tb, 0, op->stream>>>(R, S, Z, active, iters_total);
+  mx_init<<<(R * S + tb - 1) / tb, tb, 0, op->stream>>>(R, S, Z, active, iters_total, bad);
   mx_bnorm<<<R, tb, 0, op->stream>>>(R, n, bb, b.ldb, bnorm);
   op->last_launches += 2;
   // round 0 right-hand side: b itself
@@ -80,8 +81,8 @@ sgw_status solve_mixed(sgw_operator* op, const BatchDev& b, int refine_max, doub
     BatchDev bf{R, S, b.lmax, b.max_iter, b.history_iters, kRoundRelThreshold, r32, npwx, b.sigma, b.lds, y32,
                 npwx, (long long)S * npwx, b.ierr, iters_round, active, zeta, round > 0 ? 1 : 0};
     if ((s = run_msbicg<float>(op, bf)) != SGW_OK) return s;
-    mx_accumulate<<<std::min(4096, (int)(((long long)R * S * n + tb - 1) / tb)), tb, 0, op->stream>>>(
-        R, S, n, npwx, y32, x, b.ldx, b.ldr, Z, scale, active, round == 0);
+    mx_accumulate<<<R * S, tb, 0, op->stream>>>(R, S, n, npwx, y32, x, b.ldx, b.ldr, Z, scale, active, round == 0,
+                                                  bad);
     mx_update_z<<<(R * S + tb - 1) / tb, tb, 0, op->stream>>>(R, S, Z, zeta, active, iters_total, iters_round);
     op->last_launches += 2;
     // FP64 true residual of the seed system
@@ -104,7 +105,7 @@ sgw_status solve_mixed(sgw_operator* op, const BatchDev& b, int refine_max, doub
     });
     if (s != SGW_OK) return s;
   }
-  mx_finish<<<R, tb, 0, op->stream>>>(R, S, n, x, b.ldx, b.ldr, active, b.ierr, all_done ? 0 : 1);
+  mx_finish<<<(R + tb - 1) / tb, tb, 0, op->stream>>>(R, active, bad, b.ierr, all_done ? 0 : 1);
   op->last_launches += 1;
   SGW_CK(cudaGetLastError());
   return SGW_OK;

@@ -31,15 +31,12 @@
 namespace sgw {
 
 constexpr int kMaxL = 16;
-// CTA size: 256 threads, so a thread may hold up to 255 registers (a whole
-// FFT line in the register path).
 // Solver CTAs: 256 threads, one per SM, in both precisions.  (Two 128-thread
 // FP32 CTAs per SM - same register budget per thread, half the shared memory
 // each - measured 11% slower on the production system: the apply throughput
 // per SM did not change and the CTA-wide vector work got slower.)
 template <typename T> struct CtaThreads { static constexpr int v = 256; };
 template <typename T> struct CtasPerSm { static constexpr int v = 1; };
-constexpr int kThreads = 512;
 
 template <typename T>
 struct SolverArgs {

@@ -182,6 +182,7 @@ struct sgw_multi {
     int* active;
     int* iters_round;
     int* nactive;
+    int* bad;
   };
   std::vector<MixedSys> ms;
   std::vector<int> npwx;
@@ -475,7 +476,7 @@ sgw_status enqueue(sgw_multi* P) {
     const auto& m = P->ms[i];
     const int R = d.nrhs, S = d.num_shift, n = P->ops[i]->n, npwx = P->ops[i]->npwx;
     if (R == 0) continue;
-    mx_init<<<(R * S + tb - 1) / tb, tb, 0, P->stream>>>(R, S, m.Z, m.active, d.iters);
+    mx_init<<<(R * S + tb - 1) / tb, tb, 0, P->stream>>>(R, S, m.Z, m.active, d.iters, m.bad);
     mx_bnorm<<<R, tb, 0, P->stream>>>(R, n, reinterpret_cast<const zcd*>(d.bb), d.ldb, m.bnorm);
     SGW_CK(cudaMemcpy2DAsync(m.r64, sizeof(zcd) * npwx, d.bb, sizeof(zcd) * d.ldb, sizeof(zcd) * n, R,
                              cudaMemcpyDeviceToDevice, P->stream));
@@ -499,8 +500,8 @@ sgw_status enqueue(sgw_multi* P) {
       const auto& m = P->ms[i];
       const int R = d.nrhs, S = d.num_shift, n = P->ops[i]->n, npwx = P->ops[i]->npwx;
       if (R == 0) continue;
-      mx_accumulate<<<std::min(4096, (int)(((long long)R * S * n + tb - 1) / tb)), tb, 0, P->stream>>>(
-          R, S, n, npwx, m.y32, reinterpret_cast<zcd*>(d.xx), d.ldx, d.ldr, m.Z, m.scale, m.active, round == 0);
+      mx_accumulate<<<R * S, tb, 0, P->stream>>>(R, S, n, npwx, m.y32, reinterpret_cast<zcd*>(d.xx), d.ldx, d.ldr,
+                                                 m.Z, m.scale, m.active, round == 0, m.bad);
       mx_update_z<<<(R * S + tb - 1) / tb, tb, 0, P->stream>>>(R, S, m.Z, m.zeta, m.active, d.iters, m.iters_round);
       P->launches += 2;
     }
@@ -510,8 +511,7 @@ sgw_status enqueue(sgw_multi* P) {
     const sgw_batch_desc& d = P->d[i];
     const int R = d.nrhs;
     if (R == 0) continue;
-    mx_finish<<<R, tb, 0, P->stream>>>(R, d.num_shift, P->ops[i]->n, reinterpret_cast<const zcd*>(d.xx), d.ldx,
-                                       d.ldr, P->ms[i].active, d.ierr, 1);
+    mx_finish<<<(R + tb - 1) / tb, tb, 0, P->stream>>>(R, P->ms[i].active, P->ms[i].bad, d.ierr, 1);
     P->launches += 1;
   }
   SGW_CK(cudaGetLastError());
@@ -590,7 +590,7 @@ sgw_status multi_create(int nsys, sgw_operator* const* ops, const sgw_batch_desc
     for (int i = 0; i < nsys; ++i) {
       const size_t R = P->d[i].nrhs, S = P->d[i].num_shift, npwx = P->ops[i]->npwx;
       off[i + 1] = off[i] + al(sizeof(zcd) * R * npwx) + al(sizeof(zcf) * R * npwx) + al(sizeof(zcf) * R * S * npwx) +
-                   2 * al(sizeof(zcd) * R * S) + 2 * al(sizeof(double) * R) + 3 * al(sizeof(int) * R) + 256;
+                   2 * al(sizeof(zcd) * R * S) + 2 * al(sizeof(double) * R) + 4 * al(sizeof(int) * R) + 256;
     }
     if ((s = P->mixed.ensure(std::max<size_t>(off[nsys], 256))) != SGW_OK) return fail(s);
     P->ms.resize(nsys);
@@ -613,6 +613,7 @@ sgw_status multi_create(int nsys, sgw_operator* const* ops, const sgw_batch_desc
       m.active = reinterpret_cast<int*>(take(sizeof(int) * R));
       m.iters_round = reinterpret_cast<int*>(take(sizeof(int) * R));
       m.nactive = reinterpret_cast<int*>(take(sizeof(int) * R));
+      m.bad = reinterpret_cast<int*>(take(sizeof(int) * R));
     }
     s = build_solve_groups<float>(P, P->solve_groups, P->vec, P->coef, P->col, [&](int i) {
       const sgw_batch_desc& d = P->d[i];

@@ -35,24 +35,30 @@ __global__ void mx_normalise(int nrhs, int n, int npwx, const zcd* r, long long 
     o[g] = g < n ? zcf{(float)(v[g].re * inv), (float)(v[g].im * inv)} : zcf{0.f, 0.f};
 }
 
-// x^sigma += scale Z^sigma y^sigma for active right-hand sides
+// x^sigma += scale Z^sigma y^sigma for active right-hand sides, one block per
+// (right-hand side, shift) row; a non-finite term flags its right-hand side
+// (every element of x is a sum of such terms, so this replaces a NaN scan of x).
 __global__ void mx_accumulate(int nrhs, int S, int n, int npwx, const zcf* y, zcd* x, long long ldx, long long ldr,
-                              const zcd* Z, const double* scale, const int* active, bool first) {
-  const long long total = (long long)nrhs * S * n;
-  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total; e += (long long)gridDim.x * blockDim.x) {
-    const int g = (int)(e % n);
-    const long long rs = e / n;
-    const int s = (int)(rs % S), rhs = (int)(rs / S);
-    zcd* dst = x + (size_t)rhs * ldr + (size_t)s * ldx + g;
-    if (!active[rhs]) {  // a zero right-hand side never becomes active: its solution is zero
-      if (first) *dst = zcd{0.0, 0.0};
-      continue;
-    }
-    const zcf yv = y[((size_t)rhs * S + s) * npwx + g];
-    const zcd f = scale[rhs] * Z[(size_t)rhs * S + s];
-    const zcd add = f * zcd{(double)yv.re, (double)yv.im};
-    *dst = first ? add : *dst + add;
+                              const zcd* Z, const double* scale, const int* active, bool first, int* bad) {
+  const long long row = blockIdx.x;
+  if (row >= (long long)nrhs * S) return;
+  const int rhs = (int)(row / S), s = (int)(row - (long long)rhs * S);
+  zcd* xr = x + (size_t)rhs * ldr + (size_t)s * ldx;
+  if (!active[rhs]) {  // a zero right-hand side never becomes active: its solution is zero
+    if (first)
+      for (int g = threadIdx.x; g < n; g += blockDim.x) xr[g] = zcd{0.0, 0.0};
+    return;
   }
+  const zcd f = scale[rhs] * Z[row];
+  const zcf* yr = y + (size_t)row * npwx;
+  bool nonfinite = false;
+  for (int g = threadIdx.x; g < n; g += blockDim.x) {
+    const zcf yv = yr[g];
+    const zcd add = f * zcd{(double)yv.re, (double)yv.im};
+    nonfinite |= !(isfinite(add.re) && isfinite(add.im));
+    xr[g] = first ? add : xr[g] + add;
+  }
+  if (__syncthreads_or(nonfinite) && threadIdx.x == 0) bad[rhs] = 1;
 }
 
 __global__ void mx_update_z(int nrhs, int S, zcd* Z, const zcd* zeta, const int* active, int* iters_total,
@@ -65,12 +71,13 @@ __global__ void mx_update_z(int nrhs, int S, zcd* Z, const zcd* zeta, const int*
   if (e % S == 0) iters_total[rhs] += iters_round[rhs];
 }
 
-__global__ void mx_init(int nrhs, int S, zcd* Z, int* active, int* iters_total) {
+__global__ void mx_init(int nrhs, int S, zcd* Z, int* active, int* iters_total, int* bad) {
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
   if (e < nrhs * S) Z[e] = zcd{1.0, 0.0};
   if (e < nrhs) {
     active[e] = 1;
     iters_total[e] = 0;
+    bad[e] = 0;
   }
 }
 
@@ -104,19 +111,9 @@ __global__ void mx_bnorm(int nrhs, int n, const zcd* bb, long long ldb, double* 
   if (threadIdx.x == 0) bnorm[rhs] = s;
 }
 
-__global__ void mx_finish(int nrhs, int S, int n, const zcd* x, long long ldx, long long ldr, const int* active,
-                          int* ierr, int max_rounds_hit) {
-  __shared__ int bad;
-  const int rhs = blockIdx.x;
-  if (rhs >= nrhs) return;
-  if (threadIdx.x == 0) bad = 0;
-  __syncthreads();
-  for (int e = threadIdx.x; e < S * n; e += blockDim.x) {
-    const zcd v = x[(size_t)rhs * ldr + (size_t)(e / n) * ldx + (e % n)];
-    if (v.re != v.re || v.im != v.im) bad = 1;
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) ierr[rhs] = bad ? 2 : (active[rhs] && max_rounds_hit ? 1 : 0);
+__global__ void mx_finish(int nrhs, const int* active, const int* bad, int* ierr, int max_rounds_hit) {
+  const int rhs = blockIdx.x * blockDim.x + threadIdx.x;
+  if (rhs < nrhs) ierr[rhs] = bad[rhs] ? 2 : (active[rhs] && max_rounds_hit ? 1 : 0);
 }
 
 }  // namespace

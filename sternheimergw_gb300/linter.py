@@ -11,6 +11,9 @@
   * chi_matrix    the density response on the perturbation set on the GPU
                   (sgw_chi: the average above, incdrhoscf at :489-497 and the
                   G' pick of coulomb.f90:146-151);
+  * green_function  green.f90:105-226 on the GPU (sgw_green_function: the
+                  -delta right-hand sides of every listed G', one batched solve
+                  with alpha_pv = 0, the integer-map gather into green);
   * green_rhs / green_shifts   b = -delta_{G,G'} with shifts -omega
                   (green.f90:195-207, freqbins.f90:302-323);
   * coulomb_v / w_from_chi     v = 8 pi / (Omega |q+G|^2) and
