@@ -485,12 +485,20 @@ __device__ void cta_basis_gemm(cplx<T>* y, long long ldy, bool accumulate, const
       for (int k0 = 0; k0 < K; k0 += smrows) {
         const int kc = min(smrows, K - k0);
         if (!whole) fill(k0, kc);
+        // W rows are prefetched one step ahead so their L2 latency overlaps the FMAs
+        cplx<T> wn[RB];
+#pragma unroll
+        for (int r = 0; r < RB; ++r) {
+          const int g = g0 + gl + r * GR;
+          wn[r] = g < n ? W[(size_t)k0 * npwx + g] : cplx<T>{0, 0};
+        }
         for (int kk = 0; kk < kc; ++kk) {
           cplx<T> w[RB];
 #pragma unroll
           for (int r = 0; r < RB; ++r) {
+            w[r] = wn[r];
             const int g = g0 + gl + r * GR;
-            w[r] = g < n ? W[(size_t)(k0 + kk) * npwx + g] : cplx<T>{0, 0};
+            wn[r] = (g < n && kk + 1 < kc) ? W[(size_t)(k0 + kk + 1) * npwx + g] : cplx<T>{0, 0};
           }
           const cplx<T>* ck = smbuf + (size_t)kk * P + s0 + sg;
 #pragma unroll
