@@ -131,8 +131,11 @@ sgw_status sgw_linear_solver(sgw_operator* op, double threshold, int32_t max_ite
  *   bb[r*ldb + g], sigma[r*lds + s], xx[r*ldr + s*ldx + g], ierr[r], iters[r].
  * precision 0: FP64 throughout (the plain drop-in semantics).
  * precision 1: mixed - complex64 Krylov with FP64 shift recurrences and FP64
- *              residual refinement of the seed system (see sgw_solve_batch docs
- *              in the package).
+ *              residual refinement of the seed system (the FP32 rounds use
+ *              MR cycles of at most 8).  Only the seed system's FP64 residual
+ *              is refined (to refine_threshold); the other shifts follow
+ *              through the collinear restarts, with residuals of about 1e-5
+ *              relative on ill-conditioned shifts (FP64: exact semantics).
  * history_iters: outer iterations kept per history window (0 = automatic). */
 typedef struct sgw_batch_desc {
   int32_t nrhs;

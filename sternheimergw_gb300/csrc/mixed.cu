@@ -78,7 +78,8 @@ sgw_status solve_mixed(sgw_operator* op, const BatchDev& b, int refine_max, doub
     // the correction rounds run the basis product on the tensor cores (3xTF32): their
     // solutions are scaled by |r| / |b| ~ 1e-5, so its ~4x larger rounding than
     // FP32 FMAs stays far below the refinement target
-    BatchDev bf{R, S, b.lmax, b.max_iter, b.history_iters, kRoundRelThreshold, r32, npwx, b.sigma, b.lds, y32,
+    BatchDev bf{R, S, std::min(b.lmax, kMixedMaxL), b.max_iter, b.history_iters, kRoundRelThreshold, r32, npwx,
+                b.sigma, b.lds, y32,
                 npwx, (long long)S * npwx, b.ierr, iters_round, active, zeta, round > 0 ? 1 : 0};
     if ((s = run_msbicg<float>(op, bf)) != SGW_OK) return s;
     mx_accumulate<<<R * S, tb, 0, op->stream>>>(R, S, n, npwx, y32, x, b.ldx, b.ldr, Z, scale, active, round == 0,

@@ -208,8 +208,8 @@ struct SlotNeed {
 };
 
 template <typename T>
-SlotNeed slot_need(const sgw_operator* op, const sgw_batch_desc& d, int max_iter) {
-  const int l = d.lmax, Sm1 = d.num_shift - 1, Db = 2 * l + 2;
+SlotNeed slot_need(const sgw_operator* op, const sgw_batch_desc& d, int l, int max_iter) {
+  const int Sm1 = d.num_shift - 1, Db = 2 * l + 2;
   SlotNeed s{};
   s.P = std::max(32, (Sm1 + 31) / 32 * 32);
   int Tw = d.history_iters;
@@ -245,7 +245,7 @@ sgw_status build_solve_groups(sgw_multi* P, std::vector<MultiGroup>& groups, Dev
   std::vector<SolverArgs<T>> args(ns);
   for (int i = 0; i < ns; ++i) {
     args[i] = mk(i);
-    const SlotNeed need = slot_need<T>(P->ops[i], P->d[i], args[i].max_iter);
+    const SlotNeed need = slot_need<T>(P->ops[i], P->d[i], args[i].lmax, args[i].max_iter);
     args[i].Kcap = need.Kcap;
     args[i].P = need.P;
     args[i].mode = need.mode;
@@ -620,7 +620,7 @@ sgw_status multi_create(int nsys, sgw_operator* const* ops, const sgw_batch_desc
       const auto& m = P->ms[i];
       const int npwx = P->ops[i]->npwx;
       SolverArgs<float> a{};
-      a.lmax = d.lmax;
+      a.lmax = std::min(d.lmax, kMixedMaxL);
       a.max_iter = d.max_iter;
       a.threshold = kRoundRelThreshold;
       a.nshift = d.num_shift;
