@@ -132,7 +132,7 @@ sgw_status sgw_linear_solver(sgw_operator* op, double threshold, int32_t max_ite
  * precision 0: FP64 throughout (the plain drop-in semantics).
  * precision 1: mixed - complex64 Krylov with FP64 shift recurrences and FP64
  *              residual refinement of the seed system (the FP32 rounds use
- *              MR cycles of at most 8).  Only the seed system's FP64 residual
+ *              MR cycles of at most 4).  Only the seed system's FP64 residual
  *              is refined (to refine_threshold); the other shifts follow
  *              through the collinear restarts, with residuals of about 1e-5
  *              relative on ill-conditioned shifts (FP64: exact semantics).

@@ -273,11 +273,11 @@ def test_batch_edge_cases(c0, precision):
 @pytest.mark.parametrize("lmax", [1, 2, 4, 8, 12])
 def test_mixed_lin_prob(lin_prob, dense, lmax):
     """Mixed precision on the reference's dense fixture for l = 1..12 (the FP32
-    rounds cap the MR cycle at 8): FP64 seed residual <= 1e-9 relative.  The
+    rounds cap the MR cycle at 4): FP64 seed residual <= 1e-9 relative.  The
     other shifts follow the seed through the collinear restarts without an FP64
     refinement of their own, so their residual is set by FP32 rounding times the
-    conditioning (cond ~ 200 here): measured up to 4.6e-5 at l = 4 and 4.4e-4 at
-    l = 8 on the shifts nearest the seed; the test bounds it at 1e-3."""
+    conditioning (cond ~ 200 here): measured up to 4.6e-5 on the shifts nearest
+    the seed (4.4e-4 when the FP32 rounds ran l = 8); bounded here at 1e-4."""
     a, b, sig = lin_prob
     bb = np.stack([b, b[::-1].copy()])
     sh = np.stack([sig[:12], sig[:12]])
@@ -288,4 +288,4 @@ def test_mixed_lin_prob(lin_prob, dense, lmax):
         assert residual(a, sh[r, 0], x[r, 0], bb[r]) <= 1e-9 * np.linalg.norm(bb[r])
         for k in range(12):
             r64 = residual(a, sh[r, k], x64[r, k], bb[r])
-            assert residual(a, sh[r, k], x[r, k], bb[r]) <= max(1e-3, 10 * r64), (r, k)
+            assert residual(a, sh[r, k], x[r, k], bb[r]) <= max(1e-4, 10 * r64), (r, k)
