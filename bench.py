@@ -11,7 +11,8 @@ to the absolute seed residual 1e-10 with BiCGStab(4): 1808 right-hand sides,
 Arms:
   default           the GB300 library (libsgw_gb300.so) through its C ABI;
                     ``value`` times the kernels with inputs resident in HBM,
-                    ``e2e`` the same call with pinned host buffers (copies in).
+                    ``e2e`` the same call with page-locked host buffers
+                    (sgw_host_alloc), the copies in and out inside the call.
   --impl reference  the reference algorithm on the host CPU: the C
                     restatement of bicgstab.f90 (oracle/), OpenMP over
                     right-hand sides, on a bounded sample of the same workload.
@@ -182,6 +183,24 @@ class ClockSampler:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
         return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)), "reasons": sorted(reasons),
                 "samples": len(sm)}
+
+
+def huge_page_bytes(addr, nbytes):
+    """Bytes of [addr, addr + nbytes) backed by transparent huge pages (AnonHugePages
+    of the overlapping mappings in /proc/self/smaps, which covers whole mappings)."""
+    total, hit = 0, False
+    try:
+        with open("/proc/self/smaps") as f:
+            for line in f:
+                head = line.split(None, 1)[0]
+                if "-" in head and ":" not in head:
+                    lo, hi = (int(v, 16) for v in head.split("-"))
+                    hit = lo < addr + nbytes and addr < hi
+                elif hit and line.startswith("AnonHugePages:"):
+                    total += int(line.split()[1]) * 1024
+    except (OSError, ValueError):
+        return None
+    return total
 
 
 def flush_l2(buf):
@@ -539,22 +558,38 @@ def run_gpu(args, rank, world):
         chi_ms = float(np.median(chi_times[1:]))
         chi_flops = 8.0 * (nrhs // nocc) * len(s["gpert"]) * nocc * n * len(f)
 
-    # end to end through the C ABI with pinned host buffers (mixed precision, the headline path)
-    bb_h = torch.from_numpy(bb).pin_memory()
-    sg_h = torch.from_numpy(sigma).pin_memory()
-    x_h = torch.empty((nrhs, S, n), dtype=torch.complex128).pin_memory()
-    e2e_ms = []
-    # untimed calls first: they allocate the library's host-path staging buffers and
-    # touch every page of the pinned output once (the first copy into fresh pinned
-    # pages runs at a fraction of the warm bandwidth on this host)
+    # end to end through the C ABI with page-locked host buffers from sgw_host_alloc
+    # (transparent huge pages; mixed precision, the headline path)
+    bb_h = sg.host_array(bb.shape)
+    bb_h[...] = bb
+    sg_h = sg.host_array(sigma.shape)
+    sg_h[...] = sigma
+    x_h = sg.host_array((nrhs, S, n))
+    x_huge = huge_page_bytes(x_h.ctypes.data, x_h.nbytes)
+    e2e_ms, copy_ms = [], []
+    # untimed calls first: they allocate the library's host-path staging buffers
     for _ in range(2):
-        sg.solve_batch(op, bb_h.numpy(), sg_h.numpy(), lmax=LMAX, threshold=THRESHOLD, precision=1, out=x_h.numpy())
+        sg.solve_batch(op, bb_h, sg_h, lmax=LMAX, threshold=THRESHOLD, precision=1, out=x_h)
+    # the host link alone: one plain copy of the same 4.6 GB each way between the
+    # device solution and the output buffer (CUDA events, current stream)
+    link = {}
+    xt = torch.from_numpy(x_h)
+    for name, dst, src in (("d2h_gbs", xt, xm_d), ("h2d_gbs", xm_d, xt)):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record()
+        dst.copy_(src, non_blocking=True)
+        e1.record()
+        e1.synchronize()
+        link[name] = x_h.nbytes / (e0.elapsed_time(e1) * 1e-3) / 1e9
+    del xt
     for k in range(max(1, min(args.steps, 3))):
         flush_l2(l2)
         torch.cuda.synchronize()
         t = time.time()
-        sg.solve_batch(op, bb_h.numpy(), sg_h.numpy(), lmax=LMAX, threshold=THRESHOLD, precision=1, out=x_h.numpy())
+        sg.solve_batch(op, bb_h, sg_h, lmax=LMAX, threshold=THRESHOLD, precision=1, out=x_h)
         e2e_ms.append((time.time() - t) * 1e3)
+        copy_ms.append((op.kernel_timing(6)[0], op.kernel_timing(7)[0]))
     e2e_value = world * solves / (float(np.median(e2e_ms)) * 1e-3)
     h2d = bb.nbytes + sigma.nbytes
     d2h = nrhs * S * n * 16 + nrhs * 8
@@ -602,8 +637,12 @@ def run_gpu(args, rank, world):
             "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h), "ms_per_step": float(np.median(e2e_ms)),
                     "ms_per_step_all": [float(v) for v in e2e_ms],
-                    "note": "median of the timed calls; the device-to-host copy of 4.6 GB into pinned memory "
-                            "varies between 24 ms and ~200 ms on this host"},
+                    "host_buffers": "sgw_host_alloc (page-locked, transparent huge pages)",
+                    "output_huge_page_fraction": None if x_huge is None else x_huge / x_h.nbytes,
+                    "host_link_plain_copy": link,
+                    "copy_in_ms_all": [c[0] for c in copy_ms], "copy_out_ms_all": [c[1] for c in copy_ms],
+                    "note": "median of the timed calls; into cudaHostAlloc memory (base pages) the same 4.6 GB "
+                            "result copy took 24-175 ms after a solve, into these buffers 24 ms"},
             "roofline": {"bound": "fp32", "achieved": ach32, "peak": peak32, "unit": "TFLOP/s",
                          "frac": ach32 / peak32, "traffic": NCU_DRAM_BYTES_PER_RHS["fp32"] * nrhs,
                          "traffic_unit": "bytes per launch (round 0)",

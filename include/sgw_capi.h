@@ -27,6 +27,7 @@
 #define SGW_CAPI_H
 
 #include <stdint.h>
+#include <stddef.h>
 
 #ifdef __cplusplus
 extern "C" {
@@ -389,6 +390,20 @@ typedef struct sgw_tune_result {
 
 sgw_status sgw_operator_autotune(sgw_operator* op, int32_t precision, sgw_tune_result* result);
 
+/* Page-locked host buffer for the host-memory form of the calls (memory = 0),
+ * no counterpart in the reference (its arrays are Fortran allocatables; a
+ * Fortran caller maps the pointer with c_f_pointer).  The buffer is an
+ * anonymous mapping aligned to the transparent-huge-page size and advised
+ * MADV_HUGEPAGE, zero-filled (which populates it) and registered with
+ * cudaHostRegister.  Device-to-host copies into page-locked memory of base-size
+ * pages (cudaHostAlloc) lose most of their bandwidth once a solve has swept the
+ * GPU's translation caches with its working set: a 4.6 GB result copy after a
+ * batched solve took 24-175 ms into cudaHostAlloc memory and 24 ms into this
+ * buffer.  bytes = 0 returns *ptr = NULL.  sgw_host_free takes only pointers
+ * returned by sgw_host_alloc (NULL is a no-op). */
+sgw_status sgw_host_alloc(size_t bytes, void** ptr);
+sgw_status sgw_host_free(void* ptr);
+
 /* Device time (ms) of the last solve on this handle's stream, measured with
  * CUDA events around the kernels; and the number of kernel launches it used. */
 sgw_status sgw_last_timing(sgw_operator* op, double* ms, int64_t* launches);
@@ -397,7 +412,9 @@ sgw_status sgw_last_timing(sgw_operator* op, double* ms, int64_t* launches);
  * one kernel in the last sgw_solve_batch call: kernel 0 = FP64 multishift
  * solve, 1 = FP32 multishift solve (mixed precision), 2 = FP64 seed residual
  * (mixed precision); kernel 3 = the last sgw_coulomb_rhs (both of its
- * kernels), 4 = the last sgw_chi, 5 = the last sgw_vjp. */
+ * kernels), 4 = the last sgw_chi, 5 = the last sgw_vjp; 6 = the host-to-device
+ * and 7 = the device-to-host copies of the last host-memory sgw_solve_batch
+ * (0 after a device-memory call). */
 sgw_status sgw_kernel_timing(sgw_operator* op, int32_t kernel, double* ms, int64_t* launches);
 
 /* One-line description of the last error on this thread. */

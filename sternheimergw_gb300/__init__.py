@@ -5,11 +5,11 @@ in include/sgw_capi.h).  Importing this package does not load it; the first
 solver call does, and raises if it is missing.
 """
 from .solver import (BICGSTAB_MULTI, BICGSTAB_NO_MULTI, SGW_LINEAR_SOLVER, BicgstabConfig, DenseOperator,
-                     LinearSolverConfig, PlaneWaveOperator, SelectSolverConfig, bicgstab, linear_solver,
-                     select_solver, solve_batch)
+                     LinearSolverConfig, PlaneWaveOperator, SelectSolverConfig, bicgstab, host_array,
+                     linear_solver, select_solver, solve_batch)
 from ._capi import SgwError
 from . import linter, solver
 
 __all__ = ["BICGSTAB_MULTI", "BICGSTAB_NO_MULTI", "SGW_LINEAR_SOLVER", "BicgstabConfig", "DenseOperator",
            "LinearSolverConfig", "PlaneWaveOperator", "SelectSolverConfig", "bicgstab", "linear_solver",
-           "select_solver", "solve_batch", "SgwError", "solver", "linter"]
+           "select_solver", "solve_batch", "host_array", "SgwError", "solver", "linter"]

@@ -110,6 +110,8 @@ SIGNATURES = [
     ("sgw_multi_info", C.c_int, [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
     ("sgw_multi_destroy", C.c_int, [C.c_void_p]),
     ("sgw_operator_autotune", C.c_int, [C.c_void_p, C.c_int32, C.POINTER(TuneResult)]),
+    ("sgw_host_alloc", C.c_int, [C.c_size_t, C.POINTER(C.c_void_p)]),
+    ("sgw_host_free", C.c_int, [C.c_void_p]),
     ("sgw_last_timing", C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_int64)]),
     ("sgw_kernel_timing", C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_int64)]),
     ("sgw_last_error", C.c_char_p, []),

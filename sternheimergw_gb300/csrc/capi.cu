@@ -1,8 +1,16 @@
 // C-ABI entry points of libsgw_gb300.so (declared in include/sgw_capi.h).
+#include <sys/mman.h>
+#include <unistd.h>
+
 #include <algorithm>
 #include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
 #include <map>
+#include <mutex>
 #include <string>
+#include <unordered_map>
 #include <utility>
 #include <vector>
 
@@ -122,7 +130,7 @@ static sgw_status init_common(sgw_operator* op) {
 
 // Sum the per-kernel event pairs of the finished solve (stream already synchronised).
 static void collect_kernel_times(sgw_operator* op) {
-  for (int k = 0; k < K_RHS; ++k) {  // the solve kernels; rhs and chi keep their own
+  for (int k : {K_MSBICG_F64, K_MSBICG_F32, K_RESIDUAL_F64, K_COPY_IN, K_COPY_OUT}) {  // rhs/chi/vjp keep their own
     op->kernel_ms[k] = 0.0;
     op->kernel_launches[k] = 0;
   }
@@ -393,10 +401,12 @@ static sgw_status solve_batch(sgw_operator* op, const sgw_batch_desc* d) {
     if ((s = op->st_ierr.ensure(sizeof(int) * R)) != SGW_OK) return s;
     if ((s = op->st_iters.ensure(sizeof(int) * R)) != SGW_OK) return s;
     SGW_CK(cudaEventRecord(op->ev0, op->stream));
+    const int tin = ktime_begin(op, K_COPY_IN);
     SGW_CK(cudaMemcpy2DAsync(op->st_bb.p, sizeof(zcd) * n, d->bb, sizeof(zcd) * d->ldb, sizeof(zcd) * n, R,
                              cudaMemcpyHostToDevice, op->stream));
     SGW_CK(cudaMemcpy2DAsync(op->st_sigma.p, sizeof(zcd) * S, d->sigma, sizeof(zcd) * d->lds, sizeof(zcd) * S, R,
                              cudaMemcpyHostToDevice, op->stream));
+    ktime_end(op, tin);
     b.bb = op->st_bb.p;
     b.ldb = n;
     b.sigma = op->st_sigma.as<zcd>();
@@ -408,6 +418,7 @@ static sgw_status solve_batch(sgw_operator* op, const sgw_batch_desc* d) {
     b.iters = op->st_iters.as<int>();
     s = solve_batch_device(op, b, d->precision, d->refine_max, d->refine_threshold);
     if (s != SGW_OK) return s;
+    const int tout = ktime_begin(op, K_COPY_OUT);
     if (d->ldx == n && d->ldr == (long long)S * n) {  // packed host array: one linear copy
       SGW_CK(cudaMemcpyAsync(d->xx, op->st_xx.p, sizeof(zcd) * (size_t)R * S * n, cudaMemcpyDeviceToHost,
                              op->stream));
@@ -422,6 +433,7 @@ static sgw_status solve_batch(sgw_operator* op, const sgw_batch_desc* d) {
     }
     SGW_CK(cudaMemcpyAsync(d->ierr, op->st_ierr.p, sizeof(int) * R, cudaMemcpyDeviceToHost, op->stream));
     if (d->iters) SGW_CK(cudaMemcpyAsync(d->iters, op->st_iters.p, sizeof(int) * R, cudaMemcpyDeviceToHost, op->stream));
+    ktime_end(op, tout);
     SGW_CK(cudaEventRecord(op->ev1, op->stream));
     SGW_CK(cudaStreamSynchronize(op->stream));
   }
@@ -527,6 +539,82 @@ static sgw_status apply_host(sgw_operator* op, sgw_zcomplex sigma, int m, const 
   SGW_CK(cudaMemcpy2DAsync(ax, sizeof(zcd) * ldo, op->st_misc2.p, sizeof(zcd) * npwx, sizeof(zcd) * n, m,
                            cudaMemcpyDeviceToHost, op->stream));
   SGW_CK(cudaStreamSynchronize(op->stream));
+  return SGW_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Page-locked host buffers on transparent huge pages
+// ---------------------------------------------------------------------------
+static std::mutex g_host_mu;
+static std::unordered_map<void*, size_t> g_host_bufs;  // start -> mapped length
+
+// PMD (huge page) size of the running kernel: 2 MiB with 4 KiB base pages,
+// 512 MiB with 64 KiB base pages.
+static size_t thp_size() {
+  size_t v = 0;
+  if (FILE* f = std::fopen("/sys/kernel/mm/transparent_hugepage/hpage_pmd_size", "r")) {
+    unsigned long long u = 0;
+    if (std::fscanf(f, "%llu", &u) == 1) v = (size_t)u;
+    std::fclose(f);
+  }
+  return (v == 0 || (v & (v - 1))) ? ((size_t)2 << 20) : v;
+}
+
+static sgw_status host_alloc(size_t bytes, void** ptr) {
+  if (!ptr) return arg_error("null pointer argument");
+  *ptr = nullptr;
+  if (bytes == 0) return SGW_OK;
+  const size_t page = (size_t)sysconf(_SC_PAGESIZE);
+  const size_t len = (bytes + page - 1) / page * page;
+  const size_t huge = thp_size();
+  // a huge page backs only a huge-page-aligned range: map one huge page more
+  // than needed and cut the unaligned head and the tail off
+  const size_t slack = len >= huge ? huge : 0;
+  void* raw = mmap(nullptr, len + slack, PROT_READ | PROT_WRITE, MAP_PRIVATE | MAP_ANONYMOUS, -1, 0);
+  if (raw == MAP_FAILED) {
+    set_error("mmap of " + std::to_string(len) + " bytes failed");
+    return SGW_ERR_NOMEM;
+  }
+  char* p = static_cast<char*>(raw);
+  if (slack) {
+    const uintptr_t a = ((uintptr_t)raw + huge - 1) & ~(uintptr_t)(huge - 1);
+    const size_t head = a - (uintptr_t)raw;
+    if (head) munmap(raw, head);
+    if (slack - head) munmap(reinterpret_cast<char*>(a) + len, slack - head);
+    p = reinterpret_cast<char*>(a);
+  }
+  madvise(p, len, MADV_HUGEPAGE);  // advisory: base pages remain if THP is off
+  std::memset(p, 0, len);          // populate before pinning
+  const cudaError_t e = cudaHostRegister(p, len, cudaHostRegisterPortable);
+  if (e != cudaSuccess) {
+    munmap(p, len);
+    set_error(std::string("cudaHostRegister failed: ") + cudaGetErrorString(e));
+    return SGW_ERR_CUDA;
+  }
+  {
+    std::lock_guard<std::mutex> g(g_host_mu);
+    g_host_bufs[p] = len;
+  }
+  *ptr = p;
+  return SGW_OK;
+}
+
+static sgw_status host_free(void* ptr) {
+  if (!ptr) return SGW_OK;
+  size_t len = 0;
+  {
+    std::lock_guard<std::mutex> g(g_host_mu);
+    auto it = g_host_bufs.find(ptr);
+    if (it == g_host_bufs.end()) return arg_error("sgw_host_free: pointer not from sgw_host_alloc");
+    len = it->second;
+    g_host_bufs.erase(it);
+  }
+  const cudaError_t e = cudaHostUnregister(ptr);
+  munmap(ptr, len);
+  if (e != cudaSuccess) {
+    set_error(std::string("cudaHostUnregister failed: ") + cudaGetErrorString(e));
+    return SGW_ERR_CUDA;
+  }
   return SGW_OK;
 }
 
@@ -686,6 +774,17 @@ sgw_status sgw_kernel_timing(sgw_operator* op, int32_t kernel, double* ms, int64
   if (launches) *launches = op->kernel_launches[kernel];
   return SGW_OK;
 }
+
+sgw_status sgw_host_alloc(size_t bytes, void** ptr) {
+  try {
+    return host_alloc(bytes, ptr);
+  } catch (...) {
+    set_error("host exception in sgw_host_alloc");
+    return SGW_ERR_NOMEM;
+  }
+}
+
+sgw_status sgw_host_free(void* ptr) { return host_free(ptr); }
 
 const char* sgw_last_error(void) { return g_error.c_str(); }
 

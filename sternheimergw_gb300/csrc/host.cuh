@@ -86,7 +86,19 @@ struct Workspace {
 };
 
 // Kernel kinds timed with CUDA events on the operator's stream.
-enum KernelKind { K_MSBICG_F64 = 0, K_MSBICG_F32 = 1, K_RESIDUAL_F64 = 2, K_RHS = 3, K_CHI = 4, K_VJP = 5, K_NUM = 6 };
+// Timed spans of the last call, by kind: the solve kernels (0-2), the caller-side
+// kernels (3-5) and the host-path copies of sgw_solve_batch (6 in, 7 out).
+enum KernelKind {
+  K_MSBICG_F64 = 0,
+  K_MSBICG_F32 = 1,
+  K_RESIDUAL_F64 = 2,
+  K_RHS = 3,
+  K_CHI = 4,
+  K_VJP = 5,
+  K_COPY_IN = 6,
+  K_COPY_OUT = 7,
+  K_NUM = 8
+};
 constexpr int kMaxTimedLaunches = 64;
 
 }  // namespace sgw

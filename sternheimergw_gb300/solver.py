@@ -103,7 +103,8 @@ class _Operator:
         return out[:, 0] if one else out
 
     def kernel_timing(self, kernel):
-        """(ms, launches) of one kernel in the last solve_batch: 0 FP64 solve, 1 FP32 solve, 2 FP64 seed residual."""
+        """(ms, launches) of one kernel in the last call: 0 FP64 solve, 1 FP32 solve, 2 FP64 seed residual,
+        3 RHS build, 4 chi, 5 vjp, 6 / 7 the copies in / out of a host-memory solve_batch."""
         ms = C.c_double(0)
         n = C.c_int64(0)
         _capi.check(_capi.lib().sgw_kernel_timing(self.handle, int(kernel), C.byref(ms), C.byref(n)), "sgw_kernel_timing")
@@ -216,6 +217,25 @@ def select_solver(config: SelectSolverConfig, AA: _Operator, bb, sigma):
 
 def _is_torch(x):
     return type(x).__module__.startswith("torch")
+
+
+def host_array(shape, dtype=np.complex128):
+    """Zero-filled numpy array in page-locked host memory on transparent huge
+    pages (sgw_host_alloc), for the host-memory form of the calls: result
+    copies into it keep the full device-to-host bandwidth after a large solve.
+    The memory is unpinned and unmapped when the array and every view of it
+    are gone."""
+    import weakref
+    dt = np.dtype(dtype)
+    shape = tuple(int(v) for v in np.atleast_1d(shape))
+    nbytes = int(np.prod(shape, dtype=np.int64)) * dt.itemsize
+    if nbytes == 0:
+        return np.zeros(shape, dtype=dt)
+    ptr = C.c_void_p()
+    _capi.check(_capi.lib().sgw_host_alloc(nbytes, C.byref(ptr)), "sgw_host_alloc")
+    raw = (C.c_char * nbytes).from_address(ptr.value)
+    weakref.finalize(raw, _capi.lib().sgw_host_free, ptr.value)
+    return np.frombuffer(raw, dtype=dt).reshape(shape)
 
 
 def solve_batch(AA: _Operator, bb, sigma, *, lmax=4, threshold=1e-4, max_iter=10000, precision=0, history_iters=0,

@@ -27,3 +27,16 @@ def test_library_exports_every_declared_symbol():
     bound = {n for n, _, _ in _capi.SIGNATURES}
     assert set(declared_functions()) <= bound
     assert lib.sgw_version().startswith(b"sgw_gb300")
+
+
+def test_host_free_contract_without_gpu():
+    """sgw_host_alloc(0) gives NULL, sgw_host_free(NULL) is a no-op and a pointer
+    that sgw_host_alloc did not return is an argument error (host logic only)."""
+    from sternheimergw_gb300 import _capi
+    lib = _capi.lib()
+    p = ctypes.c_void_p(1234)
+    assert lib.sgw_host_alloc(0, ctypes.byref(p)) == 0 and not p.value
+    assert lib.sgw_host_free(None) == 0
+    buf = ctypes.create_string_buffer(64)
+    assert lib.sgw_host_free(ctypes.addressof(buf)) == -1
+    assert b"not from sgw_host_alloc" in lib.sgw_last_error()

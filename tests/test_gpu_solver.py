@@ -245,6 +245,35 @@ def test_large_host_batch_matches_device(lin_prob):
         assert rel(xh, xd.cpu().numpy()) < 1e-14
 
 
+def test_host_array_buffers(lin_prob):
+    """Inputs and output in sgw_host_alloc memory (huge-page, page-locked) give
+    exactly the answer of plain numpy buffers; the memory is released with the
+    array; shapes with a zero extent need no allocation."""
+    import gc
+    A, b, sigma = lin_prob
+    op = sg.DenseOperator(A)
+    rng = np.random.default_rng(13)
+    R, n = 300, A.shape[0]
+    bb = rng.standard_normal((R, n)) + 1j * rng.standard_normal((R, n))
+    sh = np.tile(sigma[:6], (R, 1))
+    bh = sg.host_array((R, n))
+    shh = sg.host_array(sh.shape)
+    xh = sg.host_array((R, 6, n))
+    assert not bh.any() and xh.flags.c_contiguous and xh.dtype == np.complex128
+    bh[...] = bb
+    shh[...] = sh
+    for prec in (0, 1):
+        x0, e0, _ = sg.solve_batch(op, bb, sh, threshold=1e-8, precision=prec)
+        _, e1, _ = sg.solve_batch(op, bh, shh, threshold=1e-8, precision=prec, out=xh)
+        assert (e0 == e1).all() and np.array_equal(x0, xh)
+    big = sg.host_array((3, 1 << 20))      # 48 MiB: spans huge-page boundaries on 4 KiB-page hosts
+    big[:, ::4096] = 1.0 + 2.0j
+    assert big.sum() == 3 * 256 * (1.0 + 2.0j)
+    del big, bh, shh, xh
+    gc.collect()
+    assert sg.host_array((0, 5)).shape == (0, 5)
+
+
 @pytest.mark.parametrize("precision", [0, 1])
 def test_batch_edge_cases(c0, precision):
     """Empty batch, a single shift, a zero right-hand side (solution 0, ierr 0), a NaN
