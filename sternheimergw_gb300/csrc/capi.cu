@@ -120,6 +120,9 @@ static sgw_status init_common(sgw_operator* op) {
   op->smem_optin = prop.sharedMemPerBlockOptin;
   op->smem_per_sm = prop.sharedMemPerMultiprocessor;
   SGW_CK(cudaStreamCreateWithFlags(&op->stream, cudaStreamNonBlocking));
+  SGW_CK(cudaStreamCreateWithFlags(&op->copy_stream, cudaStreamNonBlocking));
+  SGW_CK(cudaEventCreateWithFlags(&op->ev_acc, cudaEventDisableTiming));
+  SGW_CK(cudaEventCreateWithFlags(&op->ev_copied, cudaEventDisableTiming));
   SGW_CK(cudaEventCreate(&op->ev0));
   SGW_CK(cudaEventCreate(&op->ev1));
   SGW_CK(cudaEventCreate(&op->lev0));
@@ -355,13 +358,11 @@ static sgw_status check_batch(sgw_operator* op, const sgw_batch_desc* d) {
   return SGW_OK;
 }
 
-sgw_status solve_mixed(sgw_operator* op, const BatchDev& b, int refine_max, double refine_thr);
-
 static sgw_status solve_batch_device(sgw_operator* op, const BatchDev& b, int precision, int refine_max,
-                                     double refine_thr) {
+                                     double refine_thr, OutCopy* out = nullptr) {
   if (b.nrhs == 0) return SGW_OK;
   if (precision == 0) return run_msbicg<double>(op, b);
-  return solve_mixed(op, b, refine_max, refine_thr);
+  return solve_mixed(op, b, refine_max, refine_thr, out);
 }
 
 static sgw_status solve_batch(sgw_operator* op, const sgw_batch_desc* d) {
@@ -416,12 +417,23 @@ static sgw_status solve_batch(sgw_operator* op, const sgw_batch_desc* d) {
     b.ldr = (long long)S * n;
     b.ierr = op->st_ierr.as<int>();
     b.iters = op->st_iters.as<int>();
-    s = solve_batch_device(op, b, d->precision, d->refine_max, d->refine_threshold);
-    if (s != SGW_OK) return s;
+    // a packed host array takes one linear copy; in mixed precision it is issued
+    // on the copy stream after each accumulation and overlaps the closing residual
+    const bool packed = d->ldx == n && d->ldr == (long long)S * n;
+    OutCopy oc;
+    oc.host = d->xx;
+    oc.bytes = sizeof(zcd) * (size_t)R * S * n;
+    s = solve_batch_device(op, b, d->precision, d->refine_max, d->refine_threshold, packed ? &oc : nullptr);
+    if (s != SGW_OK) {
+      cudaStreamSynchronize(op->copy_stream);  // no copy into the caller's array outlives the call
+      return s;
+    }
+    // kind 7 times what the copies add after the solve (the part not overlapped)
     const int tout = ktime_begin(op, K_COPY_OUT);
-    if (d->ldx == n && d->ldr == (long long)S * n) {  // packed host array: one linear copy
-      SGW_CK(cudaMemcpyAsync(d->xx, op->st_xx.p, sizeof(zcd) * (size_t)R * S * n, cudaMemcpyDeviceToHost,
-                             op->stream));
+    if (oc.issued) {
+      SGW_CK(cudaStreamWaitEvent(op->stream, op->ev_copied, 0));
+    } else if (packed) {
+      SGW_CK(cudaMemcpyAsync(d->xx, op->st_xx.p, oc.bytes, cudaMemcpyDeviceToHost, op->stream));
     } else if (d->ldr == (long long)S * d->ldx) {  // one copy: every (rhs, shift) row at a uniform host pitch
       SGW_CK(cudaMemcpy2DAsync(d->xx, sizeof(zcd) * d->ldx, op->st_xx.p, sizeof(zcd) * n, sizeof(zcd) * n,
                                (size_t)R * S, cudaMemcpyDeviceToHost, op->stream));
@@ -648,6 +660,7 @@ sgw_status sgw_operator_create_dense(int32_t n, const sgw_zcomplex* a, int64_t l
 sgw_status sgw_operator_destroy(sgw_operator* op) {
   if (!op) return SGW_OK;
   if (op->stream) cudaStreamSynchronize(op->stream);
+  if (op->copy_stream) cudaStreamSynchronize(op->copy_stream);
   DevBuf* bufs[] = {&op->ymask, &op->zmask, &op->gcol, &op->gi3, &op->colpos, &op->i1list, &op->g2k64, &op->g2k32, &op->vrs64, &op->vrs32,
                     &op->vkb64, &op->vkb32, &op->dvan64, &op->dvan32, &op->evq64, &op->evq32, &op->tw64, &op->tw32,
                     &op->a64, &op->a32, &op->ws64.vec, &op->ws64.coef, &op->ws64.col, &op->ws64.counter,
@@ -662,6 +675,9 @@ sgw_status sgw_operator_destroy(sgw_operator* op) {
   if (op->ev1) cudaEventDestroy(op->ev1);
   if (op->lev0) cudaEventDestroy(op->lev0);
   if (op->lev1) cudaEventDestroy(op->lev1);
+  if (op->ev_acc) cudaEventDestroy(op->ev_acc);
+  if (op->ev_copied) cudaEventDestroy(op->ev_copied);
+  if (op->copy_stream) cudaStreamDestroy(op->copy_stream);
   if (op->stream) cudaStreamDestroy(op->stream);
   delete op;
   return SGW_OK;

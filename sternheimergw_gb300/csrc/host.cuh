@@ -109,6 +109,8 @@ struct sgw_operator {
   int device = 0, num_sms = 0;
   size_t smem_optin = 0, smem_per_sm = 0;
   cudaStream_t stream = nullptr;
+  cudaStream_t copy_stream = nullptr;                 // host-path result copies overlapped with the solve
+  cudaEvent_t ev_acc = nullptr, ev_copied = nullptr;  // its hand-offs (no timing)
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   cudaEvent_t lev0 = nullptr, lev1 = nullptr;  // sgw_coulomb_rhs / sgw_chi timing
   double last_ms = 0.0;
@@ -176,7 +178,18 @@ template <typename T> sgw_status run_msbicg(sgw_operator* op, const BatchDev& b)
 template <typename T> sgw_status run_sgw(sgw_operator* op, const SgwArgs<T>& a);
 template <typename T>
 sgw_status run_apply(sgw_operator* op, int m, const cplx<T>* x, long long ldi, cplx<T>* ax, long long ldo, zcd sigma);
-sgw_status solve_mixed(sgw_operator* op, const BatchDev& b, int refine_max, double refine_thr);
+// A device-to-host copy of the solutions (packed [nrhs][S][n], `bytes` long) that
+// solve_mixed issues on op->copy_stream after each FP64 accumulation, waiting
+// for the previous one before the next accumulation writes x; the last copy
+// follows the last accumulation, so it overlaps the closing FP64 residual.
+// `issued` is false when no accumulation ran (then nothing was copied); when it
+// is true the caller makes op->stream wait on op->ev_copied before using the host data.
+struct OutCopy {
+  void* host = nullptr;
+  size_t bytes = 0;
+  bool issued = false;
+};
+sgw_status solve_mixed(sgw_operator* op, const BatchDev& b, int refine_max, double refine_thr, OutCopy* out = nullptr);
 template <typename T>
 sgw_status run_msbicg_in(sgw_operator* op, const BatchDev& b, unsigned char* region, size_t region_bytes);
 }  // namespace sgw

@@ -23,7 +23,7 @@
 namespace sgw {
 
 
-sgw_status solve_mixed(sgw_operator* op, const BatchDev& b, int refine_max, double refine_thr) {
+sgw_status solve_mixed(sgw_operator* op, const BatchDev& b, int refine_max, double refine_thr, OutCopy* out) {
   const int R = b.nrhs, S = b.nshift, n = op->n, npwx = op->npwx;
   if (refine_max <= 0) refine_max = 4;
   if (refine_thr <= 0.0) refine_thr = 1e-9;
@@ -62,6 +62,7 @@ sgw_status solve_mixed(sgw_operator* op, const BatchDev& b, int refine_max, doub
   SGW_CK(cudaMemcpy2DAsync(r64, sizeof(zcd) * npwx, bb, sizeof(zcd) * b.ldb, sizeof(zcd) * n, R,
                            cudaMemcpyDeviceToDevice, op->stream));
   bool all_done = false;
+  bool copied = false;  // a copy of x is in flight or done on op->copy_stream
   for (int round = 0; round <= refine_max; ++round) {
     SGW_CK(cudaMemsetAsync(nactive, 0, sizeof(int), op->stream));
     mx_normalise<<<R, tb, 0, op->stream>>>(R, n, npwx, r64, npwx, r32, scale, round == 0 ? nullptr : bnorm,
@@ -71,6 +72,10 @@ sgw_status solve_mixed(sgw_operator* op, const BatchDev& b, int refine_max, doub
     SGW_CK(cudaMemcpyAsync(&h_active, nactive, sizeof(int), cudaMemcpyDeviceToHost, op->stream));
     SGW_CK(cudaStreamSynchronize(op->stream));
     if (h_active == 0) {
+      if (round == 0) {  // every right-hand side is zero: so is every solution
+        mx_accumulate<<<R * S, tb, 0, op->stream>>>(R, S, n, npwx, y32, x, b.ldx, b.ldr, Z, scale, active, true, bad);
+        op->last_launches += 1;
+      }
       all_done = true;
       break;
     }
@@ -82,10 +87,18 @@ sgw_status solve_mixed(sgw_operator* op, const BatchDev& b, int refine_max, doub
                 b.sigma, b.lds, y32,
                 npwx, (long long)S * npwx, b.ierr, iters_round, active, zeta, round > 0 ? 1 : 0};
     if ((s = run_msbicg<float>(op, bf)) != SGW_OK) return s;
+    if (copied) SGW_CK(cudaStreamWaitEvent(op->stream, op->ev_copied, 0));  // the last copy still reads x
     mx_accumulate<<<R * S, tb, 0, op->stream>>>(R, S, n, npwx, y32, x, b.ldx, b.ldr, Z, scale, active, round == 0,
                                                   bad);
     mx_update_z<<<(R * S + tb - 1) / tb, tb, 0, op->stream>>>(R, S, Z, zeta, active, iters_total, iters_round);
     op->last_launches += 2;
+    if (out) {  // x may be final now: copy it out while the FP64 residual decides
+      SGW_CK(cudaEventRecord(op->ev_acc, op->stream));
+      SGW_CK(cudaStreamWaitEvent(op->copy_stream, op->ev_acc, 0));
+      SGW_CK(cudaMemcpyAsync(out->host, x, out->bytes, cudaMemcpyDeviceToHost, op->copy_stream));
+      SGW_CK(cudaEventRecord(op->ev_copied, op->copy_stream));
+      copied = true;
+    }
     // FP64 true residual of the seed system
     s = with_applier<double>(op, [&](auto A, size_t smem) -> sgw_status {
       auto kern = mx_seed_residual<decltype(A)>;
@@ -108,6 +121,7 @@ sgw_status solve_mixed(sgw_operator* op, const BatchDev& b, int refine_max, doub
   }
   mx_finish<<<(R + tb - 1) / tb, tb, 0, op->stream>>>(R, active, bad, b.ierr, all_done ? 0 : 1);
   op->last_launches += 1;
+  if (out) out->issued = copied;
   SGW_CK(cudaGetLastError());
   return SGW_OK;
 }

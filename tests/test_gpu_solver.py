@@ -266,6 +266,13 @@ def test_host_array_buffers(lin_prob):
         x0, e0, _ = sg.solve_batch(op, bb, sh, threshold=1e-8, precision=prec)
         _, e1, _ = sg.solve_batch(op, bh, shh, threshold=1e-8, precision=prec, out=xh)
         assert (e0 == e1).all() and np.array_equal(x0, xh)
+    # the mixed host path copies x out after every accumulation; stopping at the
+    # round limit (refine_max = 1) must still return the last accumulation
+    import torch
+    x1, e1, _ = sg.solve_batch(op, bh, shh, threshold=1e-8, precision=1, refine_max=1, out=xh)
+    xd, ed, _ = sg.solve_batch(op, torch.from_numpy(bb).cuda(), torch.from_numpy(sh).cuda(), threshold=1e-8,
+                               precision=1, refine_max=1)
+    assert (e1 == ed.cpu().numpy()).all() and np.array_equal(xh, xd.cpu().numpy())
     big = sg.host_array((3, 1 << 20))      # 48 MiB: spans huge-page boundaries on 4 KiB-page hosts
     big[:, ::4096] = 1.0 + 2.0j
     assert big.sum() == 3 * 256 * (1.0 + 2.0j)
@@ -297,6 +304,18 @@ def test_batch_edge_cases(c0, precision):
         assert e2[1] == 0 and np.abs(x2[1]).max() == 0.0
     x3, e3, _ = sg.solve_batch(op, bb, sh, threshold=1e-14, precision=0, max_iter=1)
     assert (e3 == 1).all()
+    if precision == 0:
+        return
+    # mixed: every right-hand side zero gives every solution exactly zero, whatever the output held
+    import torch
+    z = np.zeros_like(bb[:3])
+    xo = np.full((3, sh.shape[1], op.n), np.nan + 1j * np.nan)
+    _, ez, _ = sg.solve_batch(op, z, sh[:3], threshold=1e-10, precision=precision, out=xo)
+    assert (ez == 0).all() and not np.abs(xo).any()
+    xd = torch.full((3, sh.shape[1], op.n), float("nan"), dtype=torch.complex128, device="cuda")
+    _, ezd, _ = sg.solve_batch(op, torch.from_numpy(z).cuda(), torch.from_numpy(sh[:3]).cuda(), threshold=1e-10,
+                               precision=precision, out=xd)
+    assert (ezd.cpu().numpy() == 0).all() and not xd.abs().cpu().numpy().any()
 
 
 @pytest.mark.parametrize("lmax", [1, 2, 4, 8, 12])
