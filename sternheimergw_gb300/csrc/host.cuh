@@ -179,11 +179,12 @@ template <typename T> sgw_status run_sgw(sgw_operator* op, const SgwArgs<T>& a);
 template <typename T>
 sgw_status run_apply(sgw_operator* op, int m, const cplx<T>* x, long long ldi, cplx<T>* ax, long long ldo, zcd sigma);
 // A device-to-host copy of the solutions (packed [nrhs][S][n], `bytes` long) that
-// solve_mixed issues on op->copy_stream after each FP64 accumulation, waiting
-// for the previous one before the next accumulation writes x; the last copy
-// follows the last accumulation, so it overlaps the closing FP64 residual.
-// `issued` is false when no accumulation ran (then nothing was copied); when it
-// is true the caller makes op->stream wait on op->ev_copied before using the host data.
+// solve_mixed issues on op->copy_stream after each FP64 accumulation that may be
+// the last one, waiting for it before a later accumulation writes x; it overlaps
+// the closing FP64 residual.  `issued` is true when such a copy followed the last
+// accumulation: the caller then makes op->stream wait on op->ev_copied before
+// using the host data; otherwise the caller copies x itself (op->stream already
+// waits for any earlier copy).
 struct OutCopy {
   void* host = nullptr;
   size_t bytes = 0;

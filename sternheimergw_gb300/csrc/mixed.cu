@@ -62,7 +62,8 @@ sgw_status solve_mixed(sgw_operator* op, const BatchDev& b, int refine_max, doub
   SGW_CK(cudaMemcpy2DAsync(r64, sizeof(zcd) * npwx, bb, sizeof(zcd) * b.ldb, sizeof(zcd) * n, R,
                            cudaMemcpyDeviceToDevice, op->stream));
   bool all_done = false;
-  bool copied = false;  // a copy of x is in flight or done on op->copy_stream
+  bool copied = false;      // a copy of x was issued on op->copy_stream
+  bool copy_final = false;  // ... after the latest accumulation
   for (int round = 0; round <= refine_max; ++round) {
     SGW_CK(cudaMemsetAsync(nactive, 0, sizeof(int), op->stream));
     mx_normalise<<<R, tb, 0, op->stream>>>(R, n, npwx, r64, npwx, r32, scale, round == 0 ? nullptr : bnorm,
@@ -92,7 +93,12 @@ sgw_status solve_mixed(sgw_operator* op, const BatchDev& b, int refine_max, doub
                                                   bad);
     mx_update_z<<<(R * S + tb - 1) / tb, tb, 0, op->stream>>>(R, S, Z, zeta, active, iters_total, iters_round);
     op->last_launches += 2;
-    if (out) {  // x may be final now: copy it out while the FP64 residual decides
+    // x may be final now: copy it out while the FP64 residual decides.  A round
+    // reduces the seed residual by about kRoundRelThreshold, so round 0 ends the
+    // refinement only for targets that loose; skipping its copy keeps 4.6 GB of
+    // copy traffic away from the L2-bound FP32 solve of round 1.
+    copy_final = out && (round > 0 || refine_thr >= kRoundRelThreshold);
+    if (copy_final) {
       SGW_CK(cudaEventRecord(op->ev_acc, op->stream));
       SGW_CK(cudaStreamWaitEvent(op->copy_stream, op->ev_acc, 0));
       SGW_CK(cudaMemcpyAsync(out->host, x, out->bytes, cudaMemcpyDeviceToHost, op->copy_stream));
@@ -121,7 +127,9 @@ sgw_status solve_mixed(sgw_operator* op, const BatchDev& b, int refine_max, doub
   }
   mx_finish<<<(R + tb - 1) / tb, tb, 0, op->stream>>>(R, active, bad, b.ierr, all_done ? 0 : 1);
   op->last_launches += 1;
-  if (out) out->issued = copied;
+  // a stale copy still in flight must land before the caller's own copy of x
+  if (copied && !copy_final) SGW_CK(cudaStreamWaitEvent(op->stream, op->ev_copied, 0));
+  if (out) out->issued = copy_final;
   SGW_CK(cudaGetLastError());
   return SGW_OK;
 }
