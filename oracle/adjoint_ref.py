@@ -1,6 +1,6 @@
 """Central finite differences of the Coulomb-response loss (numpy, dense direct solves).
 
-TEST INFRASTRUCTURE ONLY: the checker of the adjoint / vector-Jacobian-product
+TEST INFRASTRUCTURE ONLY: the oracle of the adjoint / vector-Jacobian-product
 kernels.  The product never imports it.
 
 Loss:  L(V_loc, Delta V) = Re sum_(r,s) w_s <c_rs | x_rs>,

@@ -1,7 +1,7 @@
 """CPU restatement of the caller-side steps around the Coulomb solve (numpy).
 
 TEST INFRASTRUCTURE ONLY.  Only ``tests/``, ``__graft_entry__.smoke()`` and the
-CPU-baseline leg of ``bench.py`` import this module, as the checker.  The
+CPU-baseline leg of ``bench.py`` import this module, as the oracle.  The
 product computes these steps on the GPU (sgw_coulomb_rhs, sgw_chi).
 
   dvqpsi        dvqpsi_us.f90:96-132: psi_v scattered on the box with the k map

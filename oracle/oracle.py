@@ -1,7 +1,7 @@
 """ctypes front end of the CPU oracle (oracle/_build/liboracle.so).
 
 TEST INFRASTRUCTURE ONLY.  Only ``tests/``, ``__graft_entry__.smoke()`` and the
-CPU-baseline leg of ``bench.py`` import this module, and only as the checker or
+CPU-baseline leg of ``bench.py`` import this module, and only as the oracle or
 the timed CPU reference.  The product library never loads it.
 
 The C sources restate the reference solver (algo/linear_solver/src/bicgstab.f90,

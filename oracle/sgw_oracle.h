@@ -1,7 +1,7 @@
 /*
  * CPU oracle for the SternheimerGW multishift Sternheimer solve.
  *
- * TEST INFRASTRUCTURE ONLY.  This library is the checker: the parity tests,
+ * TEST INFRASTRUCTURE ONLY.  This library is the oracle: the parity tests,
  * the smoke check and the CPU-baseline leg of the benchmark call it.  The
  * product (libsgw_gb300.so) never links, loads or calls it.
  *

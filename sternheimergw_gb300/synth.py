@@ -13,7 +13,7 @@ solver (solve_linter.f90:288-337 and green.f90:38-93 via QE init_us_2/g2_kin):
   * Kleinman-Bylander projectors beta(k+q+G) and D_ii;
   * occupied states at k (psi_v, eps_v) and at k+q (evq) from a dense FP64
     diagonalisation of the same H;
-  * alpha_pv (this build's rule: 2 (eps_max - eps_min) over the occupied
+  * alpha_pv (the generator's rule: 2 (eps_max - eps_min) over the occupied
     bands, at least 1e-2 Ry, restating the role of QE setup_alpha_pv);
   * perturbations Delta V = exp(i (q+G_p).r) and frequency lists.
 """

@@ -1,4 +1,4 @@
-"""CPU checks of the adjoint oracle (oracle/adjoint_ref.py), the checker of the
+"""CPU checks of the adjoint oracle (oracle/adjoint_ref.py), the reference values of the
 GPU vector-Jacobian products:
   * its cancellation-free central difference equals the plain quotient
     [L(V+h) - L(V-h)] / 2h of dense direct solves (h = 1e-3, where rounding of
