@@ -137,6 +137,11 @@ sgw_status sgw_linear_solver(sgw_operator* op, double threshold, int32_t max_ite
  *              is refined (to refine_threshold); the other shifts follow
  *              through the collinear restarts, with residuals of about 1e-5
  *              relative on ill-conditioned shifts (FP64: exact semantics).
+ *              With host memory and a packed xx (ldx = n, ldr = S n) the
+ *              solutions are copied out on a second stream after every
+ *              correction round, overlapping the closing FP64 residual; with
+ *              page-locked xx (sgw_host_alloc) that copy costs no time, with
+ *              pageable xx each such copy blocks the calling thread.
  * history_iters: outer iterations kept per history window (0 = automatic). */
 typedef struct sgw_batch_desc {
   int32_t nrhs;
