@@ -576,6 +576,7 @@ static sgw_status host_alloc(size_t bytes, void** ptr) {
   if (!ptr) return arg_error("null pointer argument");
   *ptr = nullptr;
   if (bytes == 0) return SGW_OK;
+  if (bytes > ((size_t)1 << 62)) return arg_error("sgw_host_alloc: size out of range");
   const size_t page = (size_t)sysconf(_SC_PAGESIZE);
   const size_t len = (bytes + page - 1) / page * page;
   const size_t huge = thp_size();

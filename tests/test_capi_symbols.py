@@ -40,3 +40,5 @@ def test_host_free_contract_without_gpu():
     buf = ctypes.create_string_buffer(64)
     assert lib.sgw_host_free(ctypes.addressof(buf)) == -1
     assert b"not from sgw_host_alloc" in lib.sgw_last_error()
+    assert lib.sgw_host_alloc(ctypes.c_size_t(-1).value, ctypes.byref(p)) == -1 and not p.value
+    assert lib.sgw_host_alloc(16, None) == -1
