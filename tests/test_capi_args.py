@@ -1,0 +1,94 @@
+"""Argument checks of sgw_operator_create_pw that run before any CUDA call, so
+they are exercised without a GPU: each malformed operator description is an
+API error (SGW_ERR_ARG = -1, nothing aborts, no handle is returned), with the
+reason in sgw_last_error().  The description is the c0 system's, broken one
+field at a time."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from sternheimergw_gb300 import _capi
+
+
+@pytest.fixture(scope="module")
+def parts(c0_system):
+    s, _ = c0_system
+    return dict(
+        nl=np.ascontiguousarray(s["nl"], dtype=np.int32),
+        g2kin=np.ascontiguousarray(s["g2kin"], dtype=np.float64),
+        vrs=np.ascontiguousarray(s["vrs"], dtype=np.float64),
+        vkb=np.asfortranarray(s["vkb"], dtype=np.complex128),
+        dvan=np.ascontiguousarray(s["dvan"], dtype=np.float64),
+        evq=np.asfortranarray(s["evq"], dtype=np.complex128),
+        nr=[int(v) for v in s["nr"]], npw=int(s["npw"]), alpha_pv=float(s["alpha_pv"]))
+
+
+def desc(p, **over):
+    d = _capi.PwOperatorDesc()
+    d.npw = d.npwx = p["npw"]
+    d.nr1, d.nr2, d.nr3 = p["nr"]
+    d.nl, d.g2kin, d.vrs = p["nl"].ctypes.data, p["g2kin"].ctypes.data, p["vrs"].ctypes.data
+    d.nkb, d.vkb, d.dvan = p["vkb"].shape[1], p["vkb"].ctypes.data, p["dvan"].ctypes.data
+    d.nbnd_occ, d.evq = p["evq"].shape[1], p["evq"].ctypes.data
+    d.alpha_pv = p["alpha_pv"]
+    for k, v in over.items():
+        setattr(d, k, v)
+    return d
+
+
+def create(d):
+    h = C.c_void_p()
+    st = _capi.lib().sgw_operator_create_pw(C.byref(d), C.byref(h))
+    return st, h.value, _capi.lib().sgw_last_error().decode()
+
+
+@pytest.mark.parametrize("field, value, reason", [
+    ("npw", 0, "invalid plane-wave operator description"),
+    ("npwx", 1, "invalid plane-wave operator description"),
+    ("nr1", 0, "invalid plane-wave operator description"),
+    ("nl", None, "invalid plane-wave operator description"),
+    ("g2kin", None, "invalid plane-wave operator description"),
+    ("vrs", None, "invalid plane-wave operator description"),
+    ("nkb", -1, "invalid projector description"),
+    ("vkb", None, "invalid projector description"),
+    ("evq", None, "invalid projector description"),
+    ("nr1", 7, "2,3,5-smooth"),
+    ("nr3", 128, "2,3,5-smooth"),
+])
+def test_malformed_description_is_an_argument_error(parts, field, value, reason):
+    st, h, msg = create(desc(parts, **{field: value}))
+    assert st == -1 and not h and reason in msg
+
+
+def test_map_outside_the_box(parts):
+    nl = parts["nl"].copy()
+    nl[5] = int(np.prod(parts["nr"]))
+    st, h, msg = create(desc(parts, nl=nl.ctypes.data))
+    assert st == -1 and not h and "outside the FFT box" in msg
+    nl[5] = -1
+    st, h, msg = create(desc(parts, nl=nl.ctypes.data))
+    assert st == -1 and "outside the FFT box" in msg
+
+
+def test_duplicate_map_entry(parts):
+    nl = parts["nl"].copy()
+    nl[7] = nl[3]
+    st, h, msg = create(desc(parts, nl=nl.ctypes.data))
+    assert st == -1 and not h and "duplicate nl index" in msg
+
+
+def test_null_arguments():
+    h = C.c_void_p()
+    assert _capi.lib().sgw_operator_create_pw(None, C.byref(h)) == -1
+    assert _capi.lib().sgw_operator_destroy(None) == 0           # like free(NULL)
+
+
+def test_valid_description_needs_a_gpu(parts):
+    """Past the argument checks the call needs CUDA: without a GPU it is a CUDA
+    error, never a CPU fallback."""
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    st, h, msg = create(desc(parts))
+    assert st == -2 and not h
