@@ -92,3 +92,53 @@ def test_valid_description_needs_a_gpu(parts):
         pytest.skip("a GPU is present")
     st, h, msg = create(desc(parts))
     assert st == -2 and not h
+
+
+def test_null_handle_is_an_argument_error():
+    """Every entry point that takes an operator or plan handle rejects NULL with
+    SGW_ERR_ARG instead of aborting (the reference aborts through errore)."""
+    L = _capi.lib()
+    z = _capi.ZComplex(0.0, 0.0)
+    buf = (C.c_double * 64)()
+    ierr = C.c_int32(0)
+    ms, n64, i32 = C.c_double(0), C.c_int64(0), C.c_int32(0)
+    calls = {
+        "sgw_solve_batch": lambda: L.sgw_solve_batch(None, C.byref(_capi.BatchDesc())),
+        "sgw_solve_batch_noalloc": lambda: L.sgw_solve_batch_noalloc(None, C.byref(_capi.BatchDesc())),
+        "sgw_coulomb_rhs": lambda: L.sgw_coulomb_rhs(None, C.byref(_capi.RhsDesc())),
+        "sgw_chi": lambda: L.sgw_chi(None, C.byref(_capi.ChiDesc())),
+        "sgw_green_function": lambda: L.sgw_green_function(None, C.byref(_capi.GreenDesc())),
+        "sgw_solve_adjoint": lambda: L.sgw_solve_adjoint(None, C.byref(_capi.AdjointDesc())),
+        "sgw_vjp": lambda: L.sgw_vjp(None, C.byref(_capi.VjpDesc())),
+        "sgw_operator_set_vloc": lambda: L.sgw_operator_set_vloc(None, buf, 64),
+        "sgw_operator_set_alpha_pv": lambda: L.sgw_operator_set_alpha_pv(None, 1.0),
+        "sgw_operator_trim": lambda: L.sgw_operator_trim(None),
+        "sgw_operator_apply": lambda: L.sgw_operator_apply(None, z, 1, buf, 4, buf, 4),
+        "sgw_operator_autotune": lambda: L.sgw_operator_autotune(None, 0, C.byref(_capi.TuneResult())),
+        "sgw_bicgstab": lambda: L.sgw_bicgstab(None, 4, 1e-6, 10, buf, 4, buf, 1, buf, 4, C.byref(ierr)),
+        "sgw_linear_solver": lambda: L.sgw_linear_solver(None, 1e-6, 10, buf, 4, buf, 1, buf, 4, C.byref(ierr)),
+        "sgw_multi_run": lambda: L.sgw_multi_run(None, C.byref(ms), None),
+        "sgw_multi_info": lambda: L.sgw_multi_info(None, C.byref(n64), C.byref(i32), C.byref(i32)),
+        "sgw_last_timing": lambda: L.sgw_last_timing(None, C.byref(ms), C.byref(n64)),
+        "sgw_kernel_timing": lambda: L.sgw_kernel_timing(None, 0, C.byref(ms), C.byref(n64)),
+    }
+    for name, call in calls.items():
+        assert call() == -1, name
+    assert L.sgw_multi_create(0, None, None, None, None) == -1
+    assert L.sgw_multi_destroy(None) == 0
+
+
+def test_select_solver_priority_semantics():
+    """select_solver.f90:116-118 (no priority: an error) and :133-155 (a code
+    that matches no solver runs nothing and leaves ierr = 1)."""
+    L = _capi.lib()
+    buf = (C.c_double * 64)()
+    ierr = C.c_int32(-5)
+    cfg = _capi.SolverConfig()
+    cfg.num_priority, cfg.max_iter, cfg.threshold, cfg.bicg_lmax = 0, 10, 1e-6, 4
+    assert L.sgw_select_solver(None, C.byref(cfg), buf, 4, buf, 1, buf, 4, C.byref(ierr)) == -1
+    assert b"priority of the solvers not specified" in L.sgw_last_error()
+    cfg.num_priority = 2
+    cfg.priority[0], cfg.priority[1] = 7, 9
+    assert L.sgw_select_solver(None, C.byref(cfg), buf, 4, buf, 1, buf, 4, C.byref(ierr)) == 1
+    assert ierr.value == 1
