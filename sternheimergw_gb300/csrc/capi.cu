@@ -217,6 +217,7 @@ static sgw_status upload_pw(sgw_operator* op, const sgw_pw_operator_desc* d, con
 }
 
 static sgw_status create_pw(const sgw_pw_operator_desc* d, sgw_operator** out) {
+  if (out) *out = nullptr;
   if (!d || !out) return arg_error("null argument");
   if (d->npw < 1 || d->npwx < d->npw || d->nr1 < 1 || d->nr2 < 1 || d->nr3 < 1 || !d->nl || !d->g2kin || !d->vrs)
     return arg_error("invalid plane-wave operator description");
@@ -317,6 +318,7 @@ static sgw_status create_pw(const sgw_pw_operator_desc* d, sgw_operator** out) {
 }
 
 static sgw_status create_dense(int n, const sgw_zcomplex* a, long long lda, sgw_operator** out) {
+  if (out) *out = nullptr;
   if (!a || !out || n < 1 || lda < n) return arg_error("invalid dense operator");
   sgw_operator* op = new sgw_operator();
   op->kind = 0;

@@ -520,6 +520,7 @@ sgw_status enqueue(sgw_multi* P) {
 
 sgw_status multi_create(int nsys, sgw_operator* const* ops, const sgw_batch_desc* descs,
                         const sgw_multi_options* opt, sgw_multi** out) {
+  if (out) *out = nullptr;
   if (nsys < 1 || !ops || !descs || !out) return multi_error("invalid multi-system arguments");
   sgw_multi_options o{};
   if (opt) o = *opt;

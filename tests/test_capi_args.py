@@ -38,7 +38,7 @@ def desc(p, **over):
 
 
 def create(d):
-    h = C.c_void_p()
+    h = C.c_void_p(0x1234)          # a failed call must leave NULL, not a stale value
     st = _capi.lib().sgw_operator_create_pw(C.byref(d), C.byref(h))
     return st, h.value, _capi.lib().sgw_last_error().decode()
 
@@ -125,6 +125,10 @@ def test_null_handle_is_an_argument_error():
     for name, call in calls.items():
         assert call() == -1, name
     assert L.sgw_multi_create(0, None, None, None, None) == -1
+    plan = C.c_void_p(0x1234)
+    assert L.sgw_multi_create(0, None, None, None, C.byref(plan)) == -1 and not plan.value
+    op = C.c_void_p(0x1234)
+    assert L.sgw_operator_create_dense(0, None, 1, C.byref(op)) == -1 and not op.value
     assert L.sgw_multi_destroy(None) == 0
 
 
