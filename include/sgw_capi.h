@@ -82,7 +82,8 @@ typedef struct sgw_operator sgw_operator;
 
 /* Build the operator handle (device copies of all tables).  Replaces the QE
  * module set-up done by init_us_2 / g2_kin before each solve
- * (solve_linter.f90:315-316, green.f90:88-91). */
+ * (solve_linter.f90:315-316, green.f90:88-91).  On failure *op is NULL (as for
+ * every call that returns a handle). */
 sgw_status sgw_operator_create_pw(const sgw_pw_operator_desc* desc, sgw_operator** op);
 
 /* Dense operator A x + sigma x, the fake operator of the solver unit test
