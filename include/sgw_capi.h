@@ -98,6 +98,16 @@ sgw_status sgw_operator_destroy(sgw_operator* op);
  * every return (bicgstab.f90:272-273). */
 sgw_status sgw_operator_trim(sgw_operator* op);
 
+/* Order the handle's work after the caller's stream: every call that queues
+ * device work on the handle first makes the handle's own stream wait (through
+ * an event) for all work the caller has queued on `stream` (a cudaStream_t of
+ * the handle's device), so device-memory inputs and output initialisations
+ * queued there just before the call are complete when the solve starts.
+ * NULL (the default) means the legacy default stream.  Every call
+ * synchronises the handle's stream before it returns.  No counterpart in the
+ * reference (host-synchronous Fortran). */
+sgw_status sgw_operator_set_stream(sgw_operator* op, void* stream);
+
 /* Switch between the Coulomb operator (alpha_pv from the set-up,
  * solve_linter.f90:657-716) and the Green's-function operator (alpha_pv = 0,
  * green.f90:231-291) without rebuilding the handle. */
@@ -107,6 +117,15 @@ sgw_status sgw_operator_set_alpha_pv(sgw_operator* op, double alpha_pv);
  * operator AA of the reference (coulomb_operator / green_operator). */
 sgw_status sgw_operator_apply(sgw_operator* op, sgw_zcomplex sigma, int32_t m, const sgw_zcomplex* x, int64_t ldx_in,
                               sgw_zcomplex* ax, int64_t ldx_out);
+
+/* The same operator with a choice of kernels and memory: precision 0 runs the
+ * FP64 kernels of the plain solve, 1 the FP32 kernels of the mixed-precision
+ * rounds (x narrowed to complex64 on the device, the result widened back);
+ * memory 0 takes host vectors, 1 device vectors.  x, ax stay complex128 in
+ * both precisions.  Checks and tuning of the kernels behind AA
+ * (linear_op.f90:46-206); no other counterpart in the reference. */
+sgw_status sgw_operator_apply_ex(sgw_operator* op, int32_t precision, int32_t memory, sgw_zcomplex sigma, int32_t m,
+                                 const sgw_zcomplex* x, int64_t ldx_in, sgw_zcomplex* ax, int64_t ldx_out);
 
 /* select_solver(config, AA, bb, sigma, xx, ierr)       select_solver.f90:67-161
  * bb[n], sigma[num_shift], xx[n x num_shift] (leading dim ldx), host memory.
@@ -171,17 +190,19 @@ sgw_status sgw_solve_batch(sgw_operator* op, const sgw_batch_desc* desc);
 /* Size of the fixed device scratch array used by sgw_solve_batch_noalloc. */
 #define SGW_NOALLOC_SCRATCH_BYTES (32u * 1024u * 1024u)
 
-/* sgw_solve_batch without any device allocation, for callers that cannot call
- * cudaMalloc while they solve (code inside a captured stream, memory-capped or
- * pool-managed processes, host codes whose device budget is fixed up front).
- * No counterpart in the reference, whose solver allocates its Krylov arrays on
- * every call (bicgstab.f90:304-490).  FP64 only (precision = 0), device
- * pointers only (memory = 1); iters may be null.  All scratch comes from one
- * static device array of SGW_NOALLOC_SCRATCH_BYTES that every GPU loading the
- * library holds until exit; problems needing more scratch per right-hand side
- * are rejected with SGW_ERR_UNSUPPORTED.  Calls share that array: calls that
- * overlap on the GPU race.  The first call on a device looks the array up
- * (cudaGetSymbolAddress); make it before any stream capture. */
+/* sgw_solve_batch without any device allocation.  No counterpart in the
+ * reference, whose solver allocates its Krylov arrays on every call
+ * (bicgstab.f90:304-490).  For callers that cannot call cudaMalloc while they
+ * solve: host codes that reserve their device memory once at start-up,
+ * processes whose GPU memory is owned by another framework's pool allocator,
+ * or plug-ins under a hard per-process memory cap.  FP64 only (precision = 0),
+ * device pointers only (memory = 1); iters may be null.  All scratch comes
+ * from one static device array of SGW_NOALLOC_SCRATCH_BYTES that every GPU
+ * loading the library holds until exit; problems needing more scratch per
+ * right-hand side are rejected with SGW_ERR_UNSUPPORTED.  Calls share that
+ * array: calls that overlap on the GPU race.  The call runs on the handle's
+ * device; the first call on a device looks the array up
+ * (cudaGetSymbolAddress). */
 sgw_status sgw_solve_batch_noalloc(sgw_operator* op, const sgw_batch_desc* desc);
 
 /* Right-hand sides of the Coulomb solve, b_(p,v) = -P_c^+ (Delta V_p psi_v),

@@ -439,3 +439,17 @@ void oracle_bicgstab_many(const oracle_bicgstab_cfg* cfg, int kind, void* op, in
   }
   (void)nthreads;
 }
+
+/* m independent applies ax_i = A(sigma_i) x_i (test infrastructure: true
+ * residuals of many solutions at once), OpenMP over the vectors. */
+void oracle_apply_many(int kind, void* op, int n, int m, const double* sigma, const double* x, double* ax,
+                       int nthreads) {
+  oracle_apply_fn fn = kind == 0 ? oracle_dense_apply : oracle_pw_apply;
+#ifdef _OPENMP
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+#pragma omp parallel for schedule(dynamic, 1)
+#endif
+  for (int i = 0; i < m; ++i)
+    fn(op, sigma + (size_t)2 * i, x + (size_t)2 * n * i, ax + (size_t)2 * n * i, n);
+  (void)nthreads;
+}

@@ -63,6 +63,8 @@ def lib():
         L.oracle_gram_schmidt.argtypes = [ip, ip, ip, vp, vp]
         L.oracle_bicgstab_many.restype = None
         L.oracle_bicgstab_many.argtypes = [C.POINTER(_BicgCfg), ip, vp, ip, ip, vp, ip, vp, vp, vp, vp, ip]
+        L.oracle_apply_many.restype = None
+        L.oracle_apply_many.argtypes = [ip, vp, ip, ip, vp, vp, vp, ip]
         L.oracle_fft3d.restype = None
         L.oracle_fft3d.argtypes = [vp, ip, ip, ip, ip]
         L.oracle_pw_hpsi.restype = None
@@ -214,3 +216,26 @@ def fft3d(box, sign):
 def norm(x):
     x = _c128(x)
     return lib().oracle_norm(x.size, _ptr(x))
+
+
+def apply_many(op, sigma, x, nthreads=0):
+    """A(sigma_i) x_i for i < m (sigma: (m,), x: (m, n)), OpenMP over the vectors."""
+    x = _c128(np.atleast_2d(x))
+    sigma = _c128(np.atleast_1d(sigma))
+    if sigma.size == 1 and x.shape[0] > 1:
+        sigma = np.full(x.shape[0], sigma[0], dtype=np.complex128)
+    out = np.zeros_like(x)
+    lib().oracle_apply_many(op.kind, op.ctx, op.n, x.shape[0], _ptr(sigma), _ptr(x), _ptr(out), int(nthreads))
+    return out
+
+
+def true_residuals(op, bb, sigma, xx, nthreads=0):
+    """Relative true residuals |A(sigma_rs) x_rs - b_r| / |b_r| of solutions xx (nrhs, S, n)
+    for right-hand sides bb (nrhs, n) and shifts sigma (nrhs, S): (nrhs, S)."""
+    bb = _c128(bb)
+    xx = _c128(xx)
+    sigma = _c128(sigma)
+    R, S, n = xx.shape
+    ax = apply_many(op, sigma.reshape(-1), xx.reshape(R * S, n), nthreads).reshape(R, S, n)
+    res = np.linalg.norm(ax - bb[:, None, :], axis=2)
+    return res / np.linalg.norm(bb, axis=1)[:, None]

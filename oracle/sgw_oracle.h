@@ -94,6 +94,10 @@ void oracle_bicgstab_many(const oracle_bicgstab_cfg* cfg, int kind, void* op, in
                           const double* bb, int nshift, const double* sigma, double* xx,
                           int* ierr, int* iters, int nthreads);
 
+/* m independent applies ax_i = A(sigma_i) x_i, OpenMP over the vectors. */
+void oracle_apply_many(int kind, void* op, int n, int m, const double* sigma, const double* x, double* ax,
+                       int nthreads);
+
 double oracle_norm(int n, const double* x);
 
 #ifdef __cplusplus

@@ -88,8 +88,11 @@ SIGNATURES = [
     ("sgw_operator_create_dense", C.c_int, [C.c_int32, C.c_void_p, C.c_int64, C.POINTER(C.c_void_p)]),
     ("sgw_operator_destroy", C.c_int, [C.c_void_p]),
     ("sgw_operator_set_alpha_pv", C.c_int, [C.c_void_p, C.c_double]),
+    ("sgw_operator_set_stream", C.c_int, [C.c_void_p, C.c_void_p]),
     ("sgw_operator_trim", C.c_int, [C.c_void_p]),
     ("sgw_operator_apply", C.c_int, [C.c_void_p, ZComplex, C.c_int32, C.c_void_p, C.c_int64, C.c_void_p, C.c_int64]),
+    ("sgw_operator_apply_ex", C.c_int, [C.c_void_p, C.c_int32, C.c_int32, ZComplex, C.c_int32, C.c_void_p, C.c_int64,
+                                        C.c_void_p, C.c_int64]),
     ("sgw_select_solver", C.c_int, [C.c_void_p, C.POINTER(SolverConfig), C.c_void_p, C.c_int32, C.c_void_p, C.c_int32,
                                     C.c_void_p, C.c_int64, C.POINTER(C.c_int32)]),
     ("sgw_bicgstab", C.c_int, [C.c_void_p, C.c_int32, C.c_double, C.c_int32, C.c_void_p, C.c_int32, C.c_void_p,

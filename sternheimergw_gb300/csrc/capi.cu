@@ -123,6 +123,7 @@ static sgw_status init_common(sgw_operator* op) {
   SGW_CK(cudaStreamCreateWithFlags(&op->copy_stream, cudaStreamNonBlocking));
   SGW_CK(cudaEventCreateWithFlags(&op->ev_acc, cudaEventDisableTiming));
   SGW_CK(cudaEventCreateWithFlags(&op->ev_copied, cudaEventDisableTiming));
+  SGW_CK(cudaEventCreateWithFlags(&op->ev_caller, cudaEventDisableTiming));
   SGW_CK(cudaEventCreate(&op->ev0));
   SGW_CK(cudaEventCreate(&op->ev1));
   SGW_CK(cudaEventCreate(&op->lev0));
@@ -131,8 +132,34 @@ static sgw_status init_common(sgw_operator* op) {
   return SGW_OK;
 }
 
+sgw_status order_after(cudaStream_t stream, cudaStream_t caller, cudaEvent_t ev) {
+  if (!ev || caller == stream) return SGW_OK;
+  SGW_CK(cudaEventRecord(ev, caller));
+  SGW_CK(cudaStreamWaitEvent(stream, ev, 0));
+  return SGW_OK;
+}
+
+CallScope::CallScope(sgw_operator* op) {
+  if (!op) return;
+  if (cudaGetDevice(&prev_) != cudaSuccess) prev_ = -1;
+  if (prev_ != op->device) {
+    const cudaError_t e = cudaSetDevice(op->device);
+    if (e != cudaSuccess) {
+      set_error(std::string("cudaSetDevice(handle's device) failed: ") + cudaGetErrorString(e));
+      st_ = SGW_ERR_CUDA;
+      return;
+    }
+    dev_ = op->device;
+  }
+  st_ = order_after(op->stream, op->caller_stream, op->ev_caller);
+}
+
+CallScope::~CallScope() {
+  if (dev_ >= 0 && prev_ >= 0) cudaSetDevice(prev_);
+}
+
 // Sum the per-kernel event pairs of the finished solve (stream already synchronised).
-static void collect_kernel_times(sgw_operator* op) {
+void collect_kernel_times(sgw_operator* op) {
   for (int k : {K_MSBICG_F64, K_MSBICG_F32, K_RESIDUAL_F64, K_COPY_IN, K_COPY_OUT}) {  // rhs/chi/vjp keep their own
     op->kernel_ms[k] = 0.0;
     op->kernel_launches[k] = 0;
@@ -556,6 +583,56 @@ static sgw_status apply_host(sgw_operator* op, sgw_zcomplex sigma, int m, const 
   return SGW_OK;
 }
 
+__global__ void widen_kernel(const zcf* in, zcd* out, long long count) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < count; i += (long long)gridDim.x * blockDim.x)
+    out[i] = zcd{(double)in[i].re, (double)in[i].im};
+}
+__global__ void narrow_kernel(const zcd* in, zcf* out, long long count) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < count; i += (long long)gridDim.x * blockDim.x)
+    out[i] = zcf{(float)in[i].re, (float)in[i].im};
+}
+
+// A(sigma) x with the FP64 (precision 0) or FP32 (precision 1) operator kernels;
+// host (memory 0) or device (memory 1) complex128 vectors.  The FP32 form
+// narrows x on the device, applies the mixed-precision solve's operator and
+// widens the result.
+static sgw_status apply_ex(sgw_operator* op, int precision, int memory, sgw_zcomplex sigma, int m,
+                           const sgw_zcomplex* x, long long ldi, sgw_zcomplex* ax, long long ldo) {
+  if (!op || (m > 0 && (!x || !ax)) || m < 0 || ldi < op->n || ldo < op->n) return arg_error("invalid apply arguments");
+  if (precision != 0 && precision != 1) return arg_error("precision must be 0 (FP64) or 1 (FP32)");
+  if (memory != 0 && memory != 1) return arg_error("memory must be 0 (host) or 1 (device)");
+  if (m == 0) return SGW_OK;
+  const int n = op->n, npwx = op->npwx;
+  const long long cnt = (long long)m * npwx;
+  const cudaMemcpyKind in_kind = memory ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+  const cudaMemcpyKind out_kind = memory ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+  sgw_status s;
+  if ((s = op->st_misc.ensure(sizeof(zcd) * (size_t)cnt)) != SGW_OK) return s;
+  if ((s = op->st_misc2.ensure(sizeof(zcd) * (size_t)cnt)) != SGW_OK) return s;
+  SGW_CK(cudaMemsetAsync(op->st_misc.p, 0, sizeof(zcd) * (size_t)cnt, op->stream));
+  SGW_CK(cudaMemcpy2DAsync(op->st_misc.p, sizeof(zcd) * npwx, x, sizeof(zcd) * ldi, sizeof(zcd) * n, m, in_kind,
+                           op->stream));
+  const zcd sg{sigma.re, sigma.im};
+  const int grid = (int)std::min<long long>((cnt + 255) / 256, (long long)op->num_sms * 8);
+  if (precision == 0) {
+    s = run_apply<double>(op, m, op->st_misc.as<zcd>(), npwx, op->st_misc2.as<zcd>(), npwx, sg);
+    if (s != SGW_OK) return s;
+  } else {
+    if ((s = op->st_misc3.ensure(2 * sizeof(zcf) * (size_t)cnt)) != SGW_OK) return s;
+    zcf* x32 = op->st_misc3.as<zcf>();
+    zcf* y32 = x32 + cnt;
+    narrow_kernel<<<grid, 256, 0, op->stream>>>(op->st_misc.as<zcd>(), x32, cnt);
+    s = run_apply<float>(op, m, x32, npwx, y32, npwx, sg);
+    if (s != SGW_OK) return s;
+    widen_kernel<<<grid, 256, 0, op->stream>>>(y32, op->st_misc2.as<zcd>(), cnt);
+    SGW_CK(cudaGetLastError());
+  }
+  SGW_CK(cudaMemcpy2DAsync(ax, sizeof(zcd) * ldo, op->st_misc2.p, sizeof(zcd) * npwx, sizeof(zcd) * n, m, out_kind,
+                           op->stream));
+  SGW_CK(cudaStreamSynchronize(op->stream));
+  return SGW_OK;
+}
+
 // ---------------------------------------------------------------------------
 // Page-locked host buffers on transparent huge pages
 // ---------------------------------------------------------------------------
@@ -680,6 +757,7 @@ sgw_status sgw_operator_destroy(sgw_operator* op) {
   if (op->lev1) cudaEventDestroy(op->lev1);
   if (op->ev_acc) cudaEventDestroy(op->ev_acc);
   if (op->ev_copied) cudaEventDestroy(op->ev_copied);
+  if (op->ev_caller) cudaEventDestroy(op->ev_caller);
   if (op->copy_stream) cudaStreamDestroy(op->copy_stream);
   if (op->stream) cudaStreamDestroy(op->stream);
   delete op;
@@ -698,6 +776,12 @@ sgw_status sgw_operator_trim(sgw_operator* op) {
   return SGW_OK;
 }
 
+sgw_status sgw_operator_set_stream(sgw_operator* op, void* stream) {
+  if (!op) return arg_error("null operator");
+  op->caller_stream = stream ? static_cast<cudaStream_t>(stream) : cudaStreamLegacy;
+  return SGW_OK;
+}
+
 sgw_status sgw_operator_set_alpha_pv(sgw_operator* op, double alpha_pv) {
   if (!op) return arg_error("null operator");
   op->alpha_pv = alpha_pv;
@@ -707,9 +791,23 @@ sgw_status sgw_operator_set_alpha_pv(sgw_operator* op, double alpha_pv) {
 sgw_status sgw_operator_apply(sgw_operator* op, sgw_zcomplex sigma, int32_t m, const sgw_zcomplex* x, int64_t ldx_in,
                               sgw_zcomplex* ax, int64_t ldx_out) {
   try {
+    CallScope cs(op);
+    if (cs.status() != SGW_OK) return cs.status();
     return apply_host(op, sigma, m, x, ldx_in, ax, ldx_out);
   } catch (...) {
     set_error("host exception in sgw_operator_apply");
+    return SGW_ERR_NOMEM;
+  }
+}
+
+sgw_status sgw_operator_apply_ex(sgw_operator* op, int32_t precision, int32_t memory, sgw_zcomplex sigma, int32_t m,
+                                 const sgw_zcomplex* x, int64_t ldx_in, sgw_zcomplex* ax, int64_t ldx_out) {
+  try {
+    CallScope cs(op);
+    if (cs.status() != SGW_OK) return cs.status();
+    return apply_ex(op, precision, memory, sigma, m, x, ldx_in, ax, ldx_out);
+  } catch (...) {
+    set_error("host exception in sgw_operator_apply_ex");
     return SGW_ERR_NOMEM;
   }
 }
@@ -718,6 +816,8 @@ sgw_status sgw_bicgstab(sgw_operator* op, int32_t lmax, double threshold, int32_
                         int32_t n, const sgw_zcomplex* sigma, int32_t num_shift, sgw_zcomplex* xx, int64_t ldx,
                         int32_t* ierr) {
   try {
+    CallScope cs(op);
+    if (cs.status() != SGW_OK) return cs.status();
     sgw_status s = single_bicgstab(op, lmax, threshold, max_iter, bb, n, sigma, num_shift, xx, ldx, ierr);
     return s == SGW_OK ? (sgw_status)*ierr : s;
   } catch (...) {
@@ -730,6 +830,8 @@ sgw_status sgw_linear_solver(sgw_operator* op, double threshold, int32_t max_ite
                              const sgw_zcomplex* sigma, int32_t num_shift, sgw_zcomplex* xx, int64_t ldx,
                              int32_t* ierr) {
   try {
+    CallScope cs(op);
+    if (cs.status() != SGW_OK) return cs.status();
     sgw_status s = single_sgw(op, threshold, max_iter, bb, n, sigma, num_shift, xx, ldx, ierr);
     return s == SGW_OK ? (sgw_status)*ierr : s;
   } catch (...) {
@@ -773,6 +875,8 @@ sgw_status sgw_select_solver(sgw_operator* op, const sgw_solver_config* cfg, con
 
 sgw_status sgw_solve_batch(sgw_operator* op, const sgw_batch_desc* desc) {
   try {
+    CallScope cs(op);
+    if (cs.status() != SGW_OK) return cs.status();
     return solve_batch(op, desc);
   } catch (...) {
     set_error("host exception in sgw_solve_batch");

@@ -109,6 +109,10 @@ struct sgw_operator {
   int device = 0, num_sms = 0;
   size_t smem_optin = 0, smem_per_sm = 0;
   cudaStream_t stream = nullptr;
+  // the caller's stream (sgw_operator_set_stream; cudaStreamLegacy by default):
+  // every call makes `stream` wait for the work queued on it before its first launch
+  cudaStream_t caller_stream = cudaStreamLegacy;
+  cudaEvent_t ev_caller = nullptr;
   cudaStream_t copy_stream = nullptr;                 // host-path result copies overlapped with the solve
   cudaEvent_t ev_acc = nullptr, ev_copied = nullptr;  // its hand-offs (no timing)
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -173,6 +177,29 @@ inline int ktime_begin(sgw_operator* op, int kind) {
 inline void ktime_end(sgw_operator* op, int i) {
   if (i >= 0) cudaEventRecord(op->kev[2 * i + 1], op->stream);
 }
+
+// Prologue of every entry point that queues device work on a handle: the
+// handle's device becomes current for the call (the caller's current device is
+// restored on exit), and the handle's stream waits for everything the caller
+// has queued on its stream (sgw_operator_set_stream; the legacy default stream
+// unless set) - so inputs written and outputs initialised by the caller just
+// before the call are complete when the first kernel starts.  Every call
+// synchronises the handle's stream before it returns.
+class CallScope {
+ public:
+  explicit CallScope(sgw_operator* op);
+  ~CallScope();
+  sgw_status status() const { return st_; }
+
+ private:
+  int prev_ = -1, dev_ = -1;
+  sgw_status st_ = SGW_OK;
+};
+// Sum the per-kernel event pairs of the last call into kernel_ms / kernel_launches
+// (the handle's stream must be synchronised).
+void collect_kernel_times(sgw_operator* op);
+// `stream` waits for the work queued so far on `caller` (event `ev` is reused).
+sgw_status order_after(cudaStream_t stream, cudaStream_t caller, cudaEvent_t ev);
 
 template <typename T> sgw_status run_msbicg(sgw_operator* op, const BatchDev& b);
 template <typename T> sgw_status run_sgw(sgw_operator* op, const SgwArgs<T>& a);

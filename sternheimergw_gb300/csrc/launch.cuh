@@ -200,9 +200,11 @@ sgw_status run_msbicg_in(sgw_operator* op, const BatchDev& b, unsigned char* reg
     SGW_CK(cudaMemsetAsync(region, 0, sizeof(int), op->stream));
     return with_applier<T>(op, [&](auto A, size_t smem) -> sgw_status {
       constexpr int NT = CtaThreads<T>::v;
-    auto kern = msbicg_kernel<T, decltype(A), NT>;
+      auto kern = msbicg_kernel<T, decltype(A), NT>;
       SGW_CK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      const int t = ktime_begin(op, sizeof(T) == 8 ? K_MSBICG_F64 : K_MSBICG_F32);
       kern<<<nslots, NT, smem, op->stream>>>(a, A);
+      ktime_end(op, t);
       SGW_CK(cudaGetLastError());
       op->last_launches += 1;
       return SGW_OK;

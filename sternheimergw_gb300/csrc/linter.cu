@@ -552,6 +552,8 @@ extern "C" {
 
 sgw_status sgw_solve_adjoint(sgw_operator* op, const sgw_adjoint_desc* desc) {
   try {
+    sgw::CallScope cs(op);
+    if (cs.status() != SGW_OK) return cs.status();
     return sgw::solve_adjoint(op, desc);
   } catch (...) {
     sgw::set_error("host exception in sgw_solve_adjoint");
@@ -561,6 +563,8 @@ sgw_status sgw_solve_adjoint(sgw_operator* op, const sgw_adjoint_desc* desc) {
 
 sgw_status sgw_vjp(sgw_operator* op, const sgw_vjp_desc* desc) {
   try {
+    sgw::CallScope cs(op);
+    if (cs.status() != SGW_OK) return cs.status();
     return sgw::vjp(op, desc);
   } catch (...) {
     sgw::set_error("host exception in sgw_vjp");
@@ -570,6 +574,8 @@ sgw_status sgw_vjp(sgw_operator* op, const sgw_vjp_desc* desc) {
 
 sgw_status sgw_green_function(sgw_operator* op, const sgw_green_desc* desc) {
   try {
+    sgw::CallScope cs(op);
+    if (cs.status() != SGW_OK) return cs.status();
     return sgw::green_function(op, desc);
   } catch (...) {
     sgw::set_error("host exception in sgw_green_function");
@@ -579,6 +585,8 @@ sgw_status sgw_green_function(sgw_operator* op, const sgw_green_desc* desc) {
 
 sgw_status sgw_operator_set_vloc(sgw_operator* op, const double* vrs, int64_t nnr) {
   try {
+    sgw::CallScope cs(op);
+    if (cs.status() != SGW_OK) return cs.status();
     return sgw::set_vloc(op, vrs, nnr);
   } catch (...) {
     sgw::set_error("host exception in sgw_operator_set_vloc");
@@ -589,6 +597,8 @@ sgw_status sgw_operator_set_vloc(sgw_operator* op, const double* vrs, int64_t nn
 
 sgw_status sgw_coulomb_rhs(sgw_operator* op, const sgw_rhs_desc* desc) {
   try {
+    sgw::CallScope cs(op);
+    if (cs.status() != SGW_OK) return cs.status();
     return sgw::coulomb_rhs(op, desc);
   } catch (...) {
     sgw::set_error("host exception in sgw_coulomb_rhs");
@@ -598,6 +608,8 @@ sgw_status sgw_coulomb_rhs(sgw_operator* op, const sgw_rhs_desc* desc) {
 
 sgw_status sgw_chi(sgw_operator* op, const sgw_chi_desc* desc) {
   try {
+    sgw::CallScope cs(op);
+    if (cs.status() != SGW_OK) return cs.status();
     return sgw::chi(op, desc);
   } catch (...) {
     sgw::set_error("host exception in sgw_chi");

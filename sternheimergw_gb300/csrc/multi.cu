@@ -165,6 +165,7 @@ struct sgw_multi {
   sgw_multi_options opt{};
   cudaStream_t stream = nullptr;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
+  cudaEvent_t ev_caller = nullptr;  // orders the plan's stream after the caller's
   int num_sms = 0, nslots = 0;
   // solve stage (FP64 solve for precision 0, FP32 rounds for precision 1) and FP64 residual stage
   std::vector<sgw::MultiGroup> solve_groups, res_groups;
@@ -551,7 +552,8 @@ sgw_status multi_create(int nsys, sgw_operator* const* ops, const sgw_batch_desc
     return s;
   };
   if (cudaStreamCreateWithFlags(&P->stream, cudaStreamNonBlocking) != cudaSuccess ||
-      cudaEventCreate(&P->e0) != cudaSuccess || cudaEventCreate(&P->e1) != cudaSuccess) {
+      cudaEventCreate(&P->e0) != cudaSuccess || cudaEventCreate(&P->e1) != cudaSuccess ||
+      cudaEventCreateWithFlags(&P->ev_caller, cudaEventDisableTiming) != cudaSuccess) {
     set_error("stream/event creation failed");
     return fail(SGW_ERR_CUDA);
   }
@@ -673,6 +675,11 @@ sgw_status multi_create(int nsys, sgw_operator* const* ops, const sgw_batch_desc
 sgw_status multi_run(sgw_multi* P, double* total_ms, double* sys_ms) {
   if (!P) return multi_error("null plan");
   std::lock_guard<std::mutex> lk(g_const_mutex);
+  // the plan's device and the caller's stream of its first system's handle
+  CallScope cs(P->ops[0]);
+  if (cs.status() != SGW_OK) return cs.status();
+  sgw_status so = order_after(P->stream, P->ops[0]->caller_stream, P->ev_caller);
+  if (so != SGW_OK) return so;
   SGW_CK(cudaEventRecord(P->e0, P->stream));
   if (P->gexec) {
     SGW_CK(cudaGraphLaunch(P->gexec, P->stream));
@@ -827,6 +834,8 @@ extern "C" {
 sgw_status sgw_multi_create(int32_t nsys, sgw_operator* const* ops, const sgw_batch_desc* descs,
                             const sgw_multi_options* opt, sgw_multi** plan) {
   try {
+    sgw::CallScope cs(nsys > 0 && ops ? ops[0] : nullptr);
+    if (cs.status() != SGW_OK) return cs.status();
     return sgw::multi_create(nsys, ops, descs, opt, plan);
   } catch (...) {
     sgw::set_error("host exception in sgw_multi_create");
@@ -871,6 +880,7 @@ sgw_status sgw_multi_destroy(sgw_multi* plan) {
     b->release();
   if (plan->e0) cudaEventDestroy(plan->e0);
   if (plan->e1) cudaEventDestroy(plan->e1);
+  if (plan->ev_caller) cudaEventDestroy(plan->ev_caller);
   if (plan->stream) cudaStreamDestroy(plan->stream);
   delete plan;
   return SGW_OK;
@@ -882,6 +892,8 @@ sgw_status sgw_operator_autotune(sgw_operator* op, int32_t precision, sgw_tune_r
       sgw::set_error("sgw_operator_autotune needs a plane-wave operator");
       return SGW_ERR_ARG;
     }
+    sgw::CallScope cs(op);
+    if (cs.status() != SGW_OK) return cs.status();
     if (precision == 0) return sgw::tune<double>(op, result);
     if (precision == 1) return sgw::tune<float>(op, result);
     sgw::set_error("precision must be 0 (FP64 kernels) or 1 (FP32 kernels)");

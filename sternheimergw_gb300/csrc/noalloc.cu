@@ -1,12 +1,14 @@
 // sgw_solve_batch_noalloc: the batched FP64 multishift solve for callers that
-// cannot allocate device memory at solve time.
+// cannot allocate device memory while they solve.
 //
-// Such callers include code running inside a captured CUDA stream, pool-managed
-// or memory-capped processes that forbid cudaMalloc after start-up, and host
-// codes (a Fortran plug-in, for instance) whose memory budget is fixed before
-// the solver runs.  They still own and pass the inputs and outputs (device
-// pointers); everything the solver needs besides them comes from one
-// fixed-size array that lives in this library's device image.
+// Some host programs fix their GPU memory before the solver runs: a Fortran
+// code that reserves its device budget at start-up, a process whose GPU
+// memory belongs to another framework's pool allocator (a cudaMalloc behind
+// the pool's back would fragment it or fail against its cap), or a plug-in
+// running under a hard per-process memory limit.  Such callers still own and
+// pass the inputs and outputs (device pointers); everything the solver needs
+// besides them comes from one fixed-size array in this library's device
+// image, so the call itself allocates nothing.
 //
 // Limits and behaviour:
 //   * the scratch array holds SGW_NOALLOC_SCRATCH_BYTES (32 MiB); every GPU that
@@ -18,9 +20,9 @@
 //     clears what must start at zero (the work counter) and the kernel
 //     initialises everything else it reads, but two calls whose work overlaps
 //     on the GPU (other streams, other threads) race on the array;
-//   * the first call on a device looks the array's address up with
-//     cudaGetSymbolAddress (once per device, with that device current); make
-//     that first call before any stream capture.
+//   * the call runs on the handle's device (made current for the call), and
+//     the first call on a device looks the array's address up with
+//     cudaGetSymbolAddress (once per device, with that device current).
 #include <mutex>
 
 #include "host.cuh"
@@ -86,12 +88,17 @@ extern "C" sgw_status sgw_solve_batch_noalloc(sgw_operator* op, const sgw_batch_
     return SGW_ERR_ARG;
   }
   if (d->nrhs == 0) return SGW_OK;
+  // the handle's device is current from here on, so the symbol lookup and the
+  // launch use that device's copy of the array
+  CallScope cs(op);
+  if (cs.status() != SGW_OK) return cs.status();
   unsigned char* region = nullptr;
   sgw_status s = scratch_address(&region);
   if (s != SGW_OK) return s;
   BatchDev b{d->nrhs, d->num_shift, d->lmax, d->max_iter, d->history_iters, d->threshold, d->bb, d->ldb,
              reinterpret_cast<const zcd*>(d->sigma), d->lds, d->xx, d->ldx, d->ldr, d->ierr, d->iters};
   op->last_launches = 0;
+  op->kev_used = 0;
   SGW_CK(cudaEventRecord(op->ev0, op->stream));
   s = run_msbicg_in<double>(op, b, region, SGW_NOALLOC_SCRATCH_BYTES);
   if (s != SGW_OK) return s;
@@ -100,5 +107,6 @@ extern "C" sgw_status sgw_solve_batch_noalloc(sgw_operator* op, const sgw_batch_
   float ms = 0.f;
   SGW_CK(cudaEventElapsedTime(&ms, op->ev0, op->ev1));
   op->last_ms = ms;
+  collect_kernel_times(op);
   return SGW_OK;
 }

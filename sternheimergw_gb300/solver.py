@@ -102,6 +102,26 @@ class _Operator:
                                                    xm.shape[1], _p(xm), self.n, _p(out), self.n), "sgw_operator_apply")
         return out[:, 0] if one else out
 
+    def apply_prec(self, sigma, x, precision=0):
+        """A(sigma) x with the FP64 (precision 0) or FP32 (precision 1) operator kernels
+        (sgw_operator_apply_ex); x of shape (n,) or (m, n) (numpy, or a CUDA torch tensor
+        that stays on the device).  Returns the same shape."""
+        z = _capi.ZComplex(complex(sigma).real, complex(sigma).imag)
+        if _is_torch(x):
+            import torch
+            xm = x.reshape(-1, self.n).contiguous()
+            out = torch.empty_like(xm)
+            _order_after_torch(self)
+            _capi.check(_capi.lib().sgw_operator_apply_ex(self.handle, int(precision), 1, z, xm.shape[0],
+                                                          xm.data_ptr(), self.n, out.data_ptr(), self.n),
+                        "sgw_operator_apply_ex")
+            return out.reshape(x.shape)
+        xm = np.ascontiguousarray(np.asarray(x, dtype=np.complex128).reshape(-1, self.n))
+        out = np.empty_like(xm)
+        _capi.check(_capi.lib().sgw_operator_apply_ex(self.handle, int(precision), 0, z, xm.shape[0], _p(xm), self.n,
+                                                      _p(out), self.n), "sgw_operator_apply_ex")
+        return out.reshape(np.shape(x))
+
     def kernel_timing(self, kernel):
         """(ms, launches) of one kernel in the last call: 0 FP64 solve, 1 FP32 solve, 2 FP64 seed residual,
         3 RHS build, 4 chi, 5 vjp, 6 / 7 the copies in / out of a host-memory solve_batch."""
@@ -219,6 +239,15 @@ def _is_torch(x):
     return type(x).__module__.startswith("torch")
 
 
+def _order_after_torch(AA: _Operator):
+    """Make the library's calls on AA wait for the work queued on torch's current
+    stream (sgw_operator_set_stream): tensors that torch has just written or
+    filled there are complete before the first kernel of the call starts."""
+    import torch
+    _capi.check(_capi.lib().sgw_operator_set_stream(AA.handle, C.c_void_p(torch.cuda.current_stream().cuda_stream)),
+                "sgw_operator_set_stream")
+
+
 def host_array(shape, dtype=np.complex128):
     """Zero-filled numpy array in page-locked host memory on transparent huge
     pages (sgw_host_alloc), for the host-memory form of the calls: result
@@ -255,8 +284,10 @@ def solve_batch(AA: _Operator, bb, sigma, *, lmax=4, threshold=1e-4, max_iter=10
         nrhs, n = bb.shape
         S = sigma.shape[1]
         xx = out if out is not None else torch.empty((nrhs, S, n), dtype=torch.complex128, device=bb.device)
-        ierr = torch.zeros(nrhs, dtype=torch.int32, device=bb.device)
-        iters = torch.zeros(nrhs, dtype=torch.int32, device=bb.device)
+        # the solve writes every entry of ierr and iters
+        ierr = torch.empty(nrhs, dtype=torch.int32, device=bb.device)
+        iters = torch.empty(nrhs, dtype=torch.int32, device=bb.device)
+        _order_after_torch(AA)
         d.memory = 1
         d.bb, d.sigma, d.xx = bb.data_ptr(), sigma.data_ptr(), xx.data_ptr()
         d.ierr, d.iters = ierr.data_ptr(), iters.data_ptr()
@@ -301,6 +332,7 @@ def coulomb_rhs(AA: PlaneWaveOperator, evc, nl_k, dvbare, out=None):
         npert = dvbare.shape[0]
         nocc = evc.shape[0]
         bb = out if out is not None else torch.empty((npert * nocc, AA.n), dtype=torch.complex128, device=evc.device)
+        _order_after_torch(AA)
         d.memory = 1
         d.nl_k, d.evc, d.dvbare, d.bb = nl_k.data_ptr(), evc.data_ptr(), dvbare.data_ptr(), bb.data_ptr()
     else:
@@ -338,6 +370,7 @@ def chi(AA: _Operator, bb, xx, nbnd, shift_plus, shift_minus, weight=1.0):
         bb = bb.contiguous()
         xx = xx.contiguous()
         out = torch.empty((xx.shape[0] // nbnd, nf, bb.shape[0] // nbnd), dtype=torch.complex128, device=bb.device)
+        _order_after_torch(AA)
         d.memory = 1
         d.bb, d.xx, d.chi = bb.data_ptr(), xx.data_ptr(), out.data_ptr()
     else:
@@ -375,7 +408,8 @@ def solve_adjoint(AA: _Operator, gbar, sigma, *, lmax=4, threshold=1e-10, max_it
         sigma = sigma.contiguous()
         R, S, n = gbar.shape
         lam = torch.empty_like(gbar)
-        ierr = torch.zeros((R, S), dtype=torch.int32, device=gbar.device)
+        ierr = torch.empty((R, S), dtype=torch.int32, device=gbar.device)  # written for every system
+        _order_after_torch(AA)
         d.memory = 1
         d.sigma, d.gbar, d.lam, d.ierr = sigma.data_ptr(), gbar.data_ptr(), lam.data_ptr(), ierr.data_ptr()
     else:
@@ -422,6 +456,7 @@ def vjp(AA: PlaneWaveOperator, xx, lam, *, evc=None, nl_k=None, want_vloc=True, 
             gd = None
         if gv is not None:
             d.grad_vloc = gv.data_ptr()
+        _order_after_torch(AA)
     else:
         xx = _c128(xx)
         lam = _c128(lam)
@@ -504,6 +539,7 @@ class MultiPlan:
 
     def run(self):
         """Solve every system; returns (total_ms, per-system completion ms)."""
+        _order_after_torch(self.ops[0])
         ms = C.c_double(0)
         per = np.zeros(self.nsys, dtype=np.float64)
         _capi.check(_capi.lib().sgw_multi_run(self.handle, C.byref(ms), per.ctypes.data), "sgw_multi_run")

@@ -114,6 +114,8 @@ def test_null_handle_is_an_argument_error():
         "sgw_operator_set_alpha_pv": lambda: L.sgw_operator_set_alpha_pv(None, 1.0),
         "sgw_operator_trim": lambda: L.sgw_operator_trim(None),
         "sgw_operator_apply": lambda: L.sgw_operator_apply(None, z, 1, buf, 4, buf, 4),
+        "sgw_operator_apply_ex": lambda: L.sgw_operator_apply_ex(None, 1, 0, z, 1, buf, 4, buf, 4),
+        "sgw_operator_set_stream": lambda: L.sgw_operator_set_stream(None, None),
         "sgw_operator_autotune": lambda: L.sgw_operator_autotune(None, 0, C.byref(_capi.TuneResult())),
         "sgw_bicgstab": lambda: L.sgw_bicgstab(None, 4, 1e-6, 10, buf, 4, buf, 1, buf, 4, C.byref(ierr)),
         "sgw_linear_solver": lambda: L.sgw_linear_solver(None, 1e-6, 10, buf, 4, buf, 1, buf, 4, C.byref(ierr)),

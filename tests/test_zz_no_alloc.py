@@ -1,11 +1,14 @@
 """The allocation-free entry point sgw_solve_batch_noalloc (C ABI) against the
 regular batched solve, on two calls in a row.
 
-Callers that cannot allocate device memory at solve time (captured streams,
-memory-capped or pool-managed processes, host codes with a fixed device
-budget) use this entry point; its scratch is a fixed static device array that
-every call reuses, so the second call also checks that leftovers of the first
-do not leak into the result.  Collected last on purpose (file name)."""
+Some callers cannot allocate device memory while they solve: host codes that
+reserve their GPU memory once at start-up, processes whose GPU memory belongs
+to another framework's pool allocator, plug-ins under a hard memory cap.  This
+entry point serves them from one fixed static device array that every call
+reuses.  The two calls solve different problems (other right-hand sides and
+shifts), each checked against its own sgw_solve_batch result, so leftovers of
+the first call in the shared array cannot pass for the second call's answer.
+Collected last on purpose (file name)."""
 import ctypes as C
 
 import numpy as np
@@ -37,15 +40,20 @@ def test_noalloc_matches_batch_twice(c0_system, gpu_lib):
     from sternheimergw_gb300 import _capi, linter
     s, f = c0_system
     op = sg.PlaneWaveOperator(s)
-    bb = torch.from_numpy(linter_ref.coulomb_rhs(s, 0)).cuda()
-    sh = torch.from_numpy(linter.coulomb_shifts(s, f)).cuda()
-    ref, ierr_ref, iters_ref = sg.solve_batch(op, bb, sh, threshold=1e-10)
-    assert int(ierr_ref.max()) == 0
+    b0 = linter_ref.coulomb_rhs(s, 0)
+    sh0 = linter.coulomb_shifts(s, f)
+    rng = np.random.default_rng(7)
+    mix = rng.standard_normal((b0.shape[0], b0.shape[0])) + 1j * rng.standard_normal((b0.shape[0], b0.shape[0]))
+    problems = [(b0, sh0), (mix @ b0, sh0 - 0.05 + 0.02j)]  # the second call: other right-hand sides and shifts
     lib = _capi.lib(build_if_missing=False)
-    for call in range(2):
+    for call, (b_np, sh_np) in enumerate(problems):
+        bb = torch.from_numpy(np.ascontiguousarray(b_np)).cuda()
+        sh = torch.from_numpy(np.ascontiguousarray(sh_np)).cuda()
+        ref, ierr_ref, iters_ref = sg.solve_batch(op, bb, sh, threshold=1e-10)
+        assert int(ierr_ref.max()) == 0
         xx = torch.full_like(ref, complex(np.nan, np.nan))
         ierr = torch.full((bb.shape[0],), -7, dtype=torch.int32, device="cuda")
-        iters = torch.zeros(bb.shape[0], dtype=torch.int32, device="cuda") if call == 0 else None
+        iters = torch.full((bb.shape[0],), -7, dtype=torch.int32, device="cuda") if call == 0 else None
         d = _desc(bb, sh, xx, ierr, iters)
         st = lib.sgw_solve_batch_noalloc(op.handle, C.byref(d))
         assert st == 0, lib.sgw_last_error()
@@ -55,6 +63,8 @@ def test_noalloc_matches_batch_twice(c0_system, gpu_lib):
             assert (iters.cpu().numpy() == iters_ref.cpu().numpy()).all()
         err = (torch.linalg.vector_norm(xx - ref) / torch.linalg.vector_norm(ref)).item()
         assert err < 1e-8, (call, err)
+        ms, launches = op.kernel_timing(0)
+        assert launches == 1 and ms > 0.0  # the no-allocation call's own solve kernel
 
 
 def test_noalloc_rejects_oversize(lin_prob, gpu_lib):
