@@ -187,6 +187,43 @@ typedef struct sgw_batch_desc {
 
 sgw_status sgw_solve_batch(sgw_operator* op, const sgw_batch_desc* desc);
 
+/* Options of sgw_solve_batch_ex beyond the reference's semantics.
+ *
+ * shift_refine 0: the reference's convergence test (seed residual only,
+ *   bicgstab.f90:237,245): shifted systems stop with the seed, converged or not.
+ * shift_refine 1: the same solve, plus every shift's relative residual
+ *   estimate |r^sigma| / |b| from the collinear residuals of the shifted
+ *   method (r^sigma = Z^sigma r_seed, the residual factors tracked in FP64 and
+ *   the seed's residual recomputed in FP64) in shift_resid, and ierr per shift:
+ *   0 every shift below shift_threshold, 1 some shift above, 2 non-finite.
+ * shift_refine 2: as 1, with restart rounds until every shift is below
+ *   shift_threshold: each round takes the shift with the largest residual as
+ *   the new seed (its residual is Z^s r_seed, collinear with all others) and
+ *   runs the batched multishift solve on it for at most round_iters outer
+ *   iterations (FP64 rounds in precision 0, complex64 in precision 1), adding
+ *   the corrections to every shift.  Shifts whose matrices are nearly singular
+ *   (real frequencies inside the spectrum with a small broadening) may stay
+ *   above the target after shift_rounds rounds: their ierr is 1.
+ * warm_start 1: xx holds a starting guess x0 on entry (a previous solution of
+ *   the same shifts); the call solves for the correction from the seed's FP64
+ *   residual r0 = b - A(sigma_1) x0^1, taken as every shift's residual, and
+ *   returns x0 + correction.  The reference's iterative screening loop solves
+ *   every iteration from zero because its solver takes no starting value
+ *   (solve_linter.f90:411-414).
+ * shift_resid: optional [r*num_shift + s] output (host or device memory like
+ *   the batch's arrays), filled when shift_refine >= 1. */
+typedef struct sgw_batch_options {
+  int32_t shift_refine;
+  double shift_threshold; /* relative residual target of every shift (0 = 1e-6) */
+  int32_t shift_rounds;   /* maximum restart rounds of shift_refine 2 (0 = 3) */
+  int32_t round_iters;    /* outer iterations per restart round (0 = 6) */
+  int32_t warm_start;
+  double* shift_resid;
+} sgw_batch_options;
+
+/* sgw_solve_batch with options (opt may be NULL: identical to sgw_solve_batch). */
+sgw_status sgw_solve_batch_ex(sgw_operator* op, const sgw_batch_desc* desc, const sgw_batch_options* opt);
+
 /* Size of the fixed device scratch array used by sgw_solve_batch_noalloc. */
 #define SGW_NOALLOC_SCRATCH_BYTES (32u * 1024u * 1024u)
 

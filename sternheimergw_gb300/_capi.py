@@ -38,6 +38,11 @@ class BatchDesc(C.Structure):
                 ("iters", C.c_void_p)]
 
 
+class BatchOptions(C.Structure):
+    _fields_ = [("shift_refine", C.c_int32), ("shift_threshold", C.c_double), ("shift_rounds", C.c_int32),
+                ("round_iters", C.c_int32), ("warm_start", C.c_int32), ("shift_resid", C.c_void_p)]
+
+
 class RhsDesc(C.Structure):
     _fields_ = [("npert", C.c_int32), ("npw_k", C.c_int32), ("nl_k", C.c_void_p), ("evc", C.c_void_p),
                 ("ldk", C.c_int64), ("dvbare", C.c_void_p), ("lddv", C.c_int64), ("bb", C.c_void_p),
@@ -100,6 +105,7 @@ SIGNATURES = [
     ("sgw_linear_solver", C.c_int, [C.c_void_p, C.c_double, C.c_int32, C.c_void_p, C.c_int32, C.c_void_p, C.c_int32,
                                     C.c_void_p, C.c_int64, C.POINTER(C.c_int32)]),
     ("sgw_solve_batch", C.c_int, [C.c_void_p, C.POINTER(BatchDesc)]),
+    ("sgw_solve_batch_ex", C.c_int, [C.c_void_p, C.POINTER(BatchDesc), C.POINTER(BatchOptions)]),
     ("sgw_solve_batch_noalloc", C.c_int, [C.c_void_p, C.POINTER(BatchDesc)]),
     ("sgw_coulomb_rhs", C.c_int, [C.c_void_p, C.POINTER(RhsDesc)]),
     ("sgw_chi", C.c_int, [C.c_void_p, C.POINTER(ChiDesc)]),

@@ -394,9 +394,27 @@ static sgw_status solve_batch_device(sgw_operator* op, const BatchDev& b, int pr
   return solve_mixed(op, b, refine_max, refine_thr, out);
 }
 
-static sgw_status solve_batch(sgw_operator* op, const sgw_batch_desc* d) {
+static sgw_status to_options(const sgw_batch_options* o, BatchOptions& bo) {
+  if (!o) return SGW_OK;
+  if (o->shift_refine < 0 || o->shift_refine > 2) return arg_error("shift_refine must be 0, 1 or 2");
+  if (o->warm_start != 0 && o->warm_start != 1) return arg_error("warm_start must be 0 or 1");
+  if (o->shift_threshold < 0.0 || o->shift_rounds < 0 || o->round_iters < 0)
+    return arg_error("negative refinement option");
+  bo.shift_refine = o->shift_refine;
+  bo.shift_tol = o->shift_threshold > 0.0 ? o->shift_threshold : 1e-6;
+  bo.rounds = o->shift_rounds > 0 ? o->shift_rounds : 3;
+  bo.round_iters = o->round_iters > 0 ? o->round_iters : 6;
+  bo.warm_start = o->warm_start;
+  return SGW_OK;
+}
+
+static sgw_status solve_batch(sgw_operator* op, const sgw_batch_desc* d, const sgw_batch_options* opt = nullptr) {
   sgw_status s = check_batch(op, d);
   if (s != SGW_OK) return s;
+  BatchOptions bo;
+  if ((s = to_options(opt, bo)) != SGW_OK) return s;
+  const bool extended = opt && (bo.shift_refine > 0 || bo.warm_start);
+  double* resid_user = opt && bo.shift_refine > 0 ? opt->shift_resid : nullptr;
   op->last_launches = 0;
   op->kev_used = 0;
   if (d->nrhs == 0) {
@@ -419,7 +437,12 @@ static sgw_status solve_batch(sgw_operator* op, const sgw_batch_desc* d) {
     if ((s = op->st_iters.ensure(sizeof(int) * std::max(R, 1))) != SGW_OK) return s;
     b.iters = d->iters ? d->iters : op->st_iters.as<int>();
     SGW_CK(cudaEventRecord(op->ev0, op->stream));
-    s = solve_batch_device(op, b, d->precision, d->refine_max, d->refine_threshold);
+    if (extended) {
+      bo.resid = resid_user;
+      s = solve_batch_opts(op, b, d->precision, d->refine_max, d->refine_threshold, bo);
+    } else {
+      s = solve_batch_device(op, b, d->precision, d->refine_max, d->refine_threshold);
+    }
     if (s != SGW_OK) return s;
     SGW_CK(cudaEventRecord(op->ev1, op->stream));
     SGW_CK(cudaStreamSynchronize(op->stream));
@@ -452,7 +475,26 @@ static sgw_status solve_batch(sgw_operator* op, const sgw_batch_desc* d) {
     OutCopy oc;
     oc.host = d->xx;
     oc.bytes = sizeof(zcd) * (size_t)R * S * n;
-    s = solve_batch_device(op, b, d->precision, d->refine_max, d->refine_threshold, packed ? &oc : nullptr);
+    if (extended) {
+      if (bo.warm_start) {  // the starting guess comes in with the other inputs
+        if (packed) {
+          SGW_CK(cudaMemcpyAsync(op->st_xx.p, d->xx, oc.bytes, cudaMemcpyHostToDevice, op->stream));
+        } else {
+          for (int r = 0; r < R; ++r)
+            SGW_CK(cudaMemcpy2DAsync(op->st_xx.as<zcd>() + (size_t)r * S * n, sizeof(zcd) * n,
+                                     reinterpret_cast<const zcd*>(d->xx) + (size_t)r * d->ldr, sizeof(zcd) * d->ldx,
+                                     sizeof(zcd) * n, S, cudaMemcpyHostToDevice, op->stream));
+        }
+      }
+      if (resid_user && (s = op->st_resid.ensure(sizeof(double) * (size_t)R * S)) != SGW_OK) return s;
+      bo.resid = resid_user ? op->st_resid.as<double>() : nullptr;
+      s = solve_batch_opts(op, b, d->precision, d->refine_max, d->refine_threshold, bo);
+      if (s == SGW_OK && resid_user)
+        SGW_CK(cudaMemcpyAsync(resid_user, op->st_resid.p, sizeof(double) * (size_t)R * S, cudaMemcpyDeviceToHost,
+                               op->stream));
+    } else {
+      s = solve_batch_device(op, b, d->precision, d->refine_max, d->refine_threshold, packed ? &oc : nullptr);
+    }
     if (s != SGW_OK) {
       cudaStreamSynchronize(op->copy_stream);  // no copy into the caller's array outlives the call
       return s;
@@ -746,7 +788,7 @@ sgw_status sgw_operator_destroy(sgw_operator* op) {
                     &op->a64, &op->a32, &op->ws64.vec, &op->ws64.coef, &op->ws64.col, &op->ws64.counter,
                     &op->ws32.vec, &op->ws32.coef, &op->ws32.col, &op->ws32.counter, &op->st_bb, &op->st_sigma,
                     &op->st_xx, &op->st_ierr, &op->st_iters, &op->st_misc, &op->st_misc2, &op->st_misc3,
-                    &op->nlkq, &op->lt_psi, &op->lt_box, &op->lt_nlk, &op->lt_evc, &op->lt_dv, &op->lt_bb,
+                    &op->st_ref, &op->st_ref2, &op->st_resid, &op->nlkq, &op->lt_psi, &op->lt_box, &op->lt_nlk, &op->lt_evc, &op->lt_dv, &op->lt_bb,
                     &op->lt_flag, &op->lt_part, &op->lt_sidx, &op->lt_xx, &op->lt_chi};
   for (DevBuf* b : bufs) b->release();
   for (int i = 0; i < 2 * kMaxTimedLaunches; ++i)
@@ -769,7 +811,8 @@ sgw_status sgw_operator_trim(sgw_operator* op) {
   if (op->stream) SGW_CK(cudaStreamSynchronize(op->stream));
   DevBuf* bufs[] = {&op->ws64.vec, &op->ws64.coef, &op->ws64.col, &op->ws64.counter, &op->ws32.vec, &op->ws32.coef,
                     &op->ws32.col, &op->ws32.counter, &op->st_bb, &op->st_sigma, &op->st_xx, &op->st_ierr,
-                    &op->st_iters, &op->st_misc, &op->st_misc2, &op->st_misc3, &op->lt_psi, &op->lt_box,
+                    &op->st_iters, &op->st_misc, &op->st_misc2, &op->st_misc3, &op->st_ref, &op->st_ref2,
+                    &op->st_resid, &op->lt_psi, &op->lt_box,
                     &op->lt_nlk, &op->lt_evc, &op->lt_dv, &op->lt_bb, &op->lt_flag, &op->lt_part, &op->lt_sidx,
                     &op->lt_xx, &op->lt_chi};
   for (DevBuf* b : bufs) b->release();
@@ -880,6 +923,17 @@ sgw_status sgw_solve_batch(sgw_operator* op, const sgw_batch_desc* desc) {
     return solve_batch(op, desc);
   } catch (...) {
     set_error("host exception in sgw_solve_batch");
+    return SGW_ERR_NOMEM;
+  }
+}
+
+sgw_status sgw_solve_batch_ex(sgw_operator* op, const sgw_batch_desc* desc, const sgw_batch_options* opt) {
+  try {
+    CallScope cs(op);
+    if (cs.status() != SGW_OK) return cs.status();
+    return solve_batch(op, desc, opt);
+  } catch (...) {
+    set_error("host exception in sgw_solve_batch_ex");
     return SGW_ERR_NOMEM;
   }
 }

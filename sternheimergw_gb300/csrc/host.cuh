@@ -138,6 +138,7 @@ struct sgw_operator {
   // workspaces and staging
   sgw::Workspace ws64, ws32;
   sgw::DevBuf st_bb, st_sigma, st_xx, st_ierr, st_iters, st_misc, st_misc2, st_misc3;
+  sgw::DevBuf st_ref, st_ref2, st_resid;  // restart rounds and warm starts (sgw_solve_batch_ex)
   // right-hand-side build and chi accumulation
   sgw::DevBuf lt_psi, lt_box, lt_nlk, lt_evc, lt_dv, lt_bb, lt_flag, lt_part, lt_sidx, lt_xx, lt_chi;
 };
@@ -217,7 +218,36 @@ struct OutCopy {
   size_t bytes = 0;
   bool issued = false;
 };
-sgw_status solve_mixed(sgw_operator* op, const BatchDev& b, int refine_max, double refine_thr, OutCopy* out = nullptr);
+// What a mixed solve leaves behind (device pointers into the handle's staging
+// buffers, valid until the next call on the handle): residual factors Z with
+// shifted residual = Z^sigma r for every (right-hand side, shift), the FP64 true
+// residual r of the seed shift after the last accumulation, its norm and the
+// right-hand-side norms.
+struct RoundState {
+  zcd* Z = nullptr;
+  zcd* r64 = nullptr;
+  double* scale = nullptr;
+  double* bnorm = nullptr;
+};
+// norm_ref (optional, leading dimension norm_ld): the right-hand sides whose
+// norms set the FP64 refinement target (refine_thr |norm_ref_r|) instead of
+// b.bb's own - a warm start solves for a small correction whose accuracy is
+// measured against the full right-hand side.
+sgw_status solve_mixed(sgw_operator* op, const BatchDev& b, int refine_max, double refine_thr, OutCopy* out = nullptr,
+                       RoundState* st = nullptr, const zcd* norm_ref = nullptr, long long norm_ld = 0);
+
+// Host-side view of sgw_batch_options (defaults filled in); resid is a device
+// array [nrhs][nshift] or null.
+struct BatchOptions {
+  int shift_refine = 0;  // 0 reference semantics, 1 + per-shift estimates, 2 + restart rounds
+  double shift_tol = 1e-6;
+  int rounds = 0;
+  int round_iters = 6;
+  int warm_start = 0;
+  double* resid = nullptr;
+};
+sgw_status solve_batch_opts(sgw_operator* op, const BatchDev& b, int precision, int refine_max, double refine_thr,
+                            const BatchOptions& o);
 template <typename T>
 sgw_status run_msbicg_in(sgw_operator* op, const BatchDev& b, unsigned char* region, size_t region_bytes);
 }  // namespace sgw

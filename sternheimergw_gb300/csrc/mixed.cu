@@ -23,7 +23,8 @@
 namespace sgw {
 
 
-sgw_status solve_mixed(sgw_operator* op, const BatchDev& b, int refine_max, double refine_thr, OutCopy* out) {
+sgw_status solve_mixed(sgw_operator* op, const BatchDev& b, int refine_max, double refine_thr, OutCopy* out,
+                       RoundState* st, const zcd* norm_ref, long long norm_ld) {
   const int R = b.nrhs, S = b.nshift, n = op->n, npwx = op->npwx;
   if (refine_max <= 0) refine_max = 4;
   if (refine_thr <= 0.0) refine_thr = 1e-9;
@@ -56,7 +57,7 @@ sgw_status solve_mixed(sgw_operator* op, const BatchDev& b, int refine_max, doub
   zcd* x = reinterpret_cast<zcd*>(b.xx);
   const int tb = 256;
   mx_init<<<(R * S + tb - 1) / tb, tb, 0, op->stream>>>(R, S, Z, active, iters_total, bad);
-  mx_bnorm<<<R, tb, 0, op->stream>>>(R, n, bb, b.ldb, bnorm);
+  mx_bnorm<<<R, tb, 0, op->stream>>>(R, n, norm_ref ? norm_ref : bb, norm_ref ? norm_ld : b.ldb, bnorm);
   op->last_launches += 2;
   // round 0 right-hand side: b itself
   SGW_CK(cudaMemcpy2DAsync(r64, sizeof(zcd) * npwx, bb, sizeof(zcd) * b.ldb, sizeof(zcd) * n, R,
@@ -130,6 +131,12 @@ sgw_status solve_mixed(sgw_operator* op, const BatchDev& b, int refine_max, doub
   // a stale copy still in flight must land before the caller's own copy of x
   if (copied && !copy_final) SGW_CK(cudaStreamWaitEvent(op->stream, op->ev_copied, 0));
   if (out) out->issued = copy_final;
+  if (st) {
+    st->Z = Z;
+    st->r64 = r64;
+    st->scale = scale;
+    st->bnorm = bnorm;
+  }
   SGW_CK(cudaGetLastError());
   return SGW_OK;
 }

@@ -268,14 +268,32 @@ def host_array(shape, dtype=np.complex128):
 
 
 def solve_batch(AA: _Operator, bb, sigma, *, lmax=4, threshold=1e-4, max_iter=10000, precision=0, history_iters=0,
-                refine_max=0, refine_threshold=0.0, out=None):
+                refine_max=0, refine_threshold=0.0, out=None, shift_refine=0, shift_threshold=0.0, shift_rounds=0,
+                round_iters=0, x0=None, return_resid=False):
     """Multishift solve of nrhs right-hand sides sharing one operator.
 
     bb: (nrhs, n) complex128; sigma: (nrhs, S) complex128.  numpy arrays run
     through host memory (copies inside the call); CUDA torch tensors stay on
-    the device.  Returns (xx[nrhs, S, n], ierr[nrhs], iters[nrhs]).
+    the device.  Returns (xx[nrhs, S, n], ierr[nrhs], iters[nrhs]), plus the
+    per-shift relative residual estimates resid[nrhs, S] with return_resid.
+
+    Options of sgw_solve_batch_ex: shift_refine 0 keeps the reference's
+    seed-only convergence, 1 adds per-shift residual estimates (ierr per
+    shift), 2 adds restart rounds with seed switching until every shift is
+    below shift_threshold (default 1e-6; at most shift_rounds rounds of
+    round_iters outer iterations); x0 (nrhs, S, n) is a starting guess from a
+    previous solve of the same shifts (warm start).
     """
     d = _capi.BatchDesc()
+    opts = None
+    if shift_refine or x0 is not None or return_resid:
+        opts = _capi.BatchOptions()
+        opts.shift_refine = int(max(shift_refine, 1 if return_resid else 0))
+        opts.shift_threshold = float(shift_threshold)
+        opts.shift_rounds = int(shift_rounds)
+        opts.round_iters = int(round_iters)
+        opts.warm_start = 1 if x0 is not None else 0
+    resid = None
     if _is_torch(bb):
         import torch
         assert bb.is_cuda and sigma.is_cuda and bb.dtype == torch.complex128 and sigma.dtype == torch.complex128
@@ -284,6 +302,11 @@ def solve_batch(AA: _Operator, bb, sigma, *, lmax=4, threshold=1e-4, max_iter=10
         nrhs, n = bb.shape
         S = sigma.shape[1]
         xx = out if out is not None else torch.empty((nrhs, S, n), dtype=torch.complex128, device=bb.device)
+        if x0 is not None and x0.data_ptr() != xx.data_ptr():
+            xx.copy_(x0)
+        if opts is not None and opts.shift_refine:
+            resid = torch.empty((nrhs, S), dtype=torch.float64, device=bb.device)
+            opts.shift_resid = resid.data_ptr()
         # the solve writes every entry of ierr and iters
         ierr = torch.empty(nrhs, dtype=torch.int32, device=bb.device)
         iters = torch.empty(nrhs, dtype=torch.int32, device=bb.device)
@@ -297,6 +320,11 @@ def solve_batch(AA: _Operator, bb, sigma, *, lmax=4, threshold=1e-4, max_iter=10
         nrhs, n = bb.shape
         S = sigma.shape[1]
         xx = out if out is not None else np.zeros((nrhs, S, n), dtype=np.complex128)
+        if x0 is not None and np.asarray(x0).ctypes.data != xx.ctypes.data:
+            xx[...] = x0
+        if opts is not None and opts.shift_refine:
+            resid = np.zeros((nrhs, S), dtype=np.float64)
+            opts.shift_resid = resid.ctypes.data
         ierr = np.zeros(nrhs, dtype=np.int32)
         iters = np.zeros(nrhs, dtype=np.int32)
         d.memory = 0
@@ -311,7 +339,12 @@ def solve_batch(AA: _Operator, bb, sigma, *, lmax=4, threshold=1e-4, max_iter=10
     d.refine_max = int(refine_max)
     d.refine_threshold = float(refine_threshold)
     d.ldb, d.lds, d.ldx, d.ldr = n, S, n, S * n
-    _capi.check(_capi.lib().sgw_solve_batch(AA.handle, C.byref(d)), "sgw_solve_batch")
+    if opts is None:
+        _capi.check(_capi.lib().sgw_solve_batch(AA.handle, C.byref(d)), "sgw_solve_batch")
+    else:
+        _capi.check(_capi.lib().sgw_solve_batch_ex(AA.handle, C.byref(d), C.byref(opts)), "sgw_solve_batch_ex")
+    if return_resid:
+        return xx, ierr, iters, resid
     return xx, ierr, iters
 
 

@@ -80,8 +80,12 @@ def test_apply_c1_box(c1_system, gpu_lib):
 
 def test_multishift_c1_reduced(c1_system, gpu_lib):
     """8 right-hand sides x 70 shifts of the production system, FP64 GPU vs the
-    oracle: the seed to 1e-8; every shift whose oracle solution has converged
-    (true relative residual <= 1e-6) to 1e-7."""
+    oracle: the seed solution to 1e-8 and both seeds' residuals below the
+    absolute threshold; every shift's true relative residual within 1% (+1e-9)
+    of the oracle's (the same iterations, converged or not); solutions of
+    shifts with oracle residual <= 1e-8 to 1e-5 (two solutions with residuals
+    near 1e-8 agree only to about the shift's condition number, up to ~3e3
+    here, times that residual)."""
     import sternheimergw_gb300 as sg
     from oracle import linter_ref
     from oracle import oracle as O
@@ -97,7 +101,10 @@ def test_multishift_c1_reduced(c1_system, gpu_lib):
     seed_err = np.linalg.norm(x[:, 0] - xo[:, 0], axis=1) / np.linalg.norm(xo[:, 0], axis=1)
     assert seed_err.max() < 1e-8, seed_err
     res = O.true_residuals(oop, bb, sh, xo)
-    ok = res <= 1e-6
-    assert ok[:, 0].all()
+    res_gpu = O.true_residuals(oop, bb, sh, x)
+    bnorm = np.linalg.norm(bb, axis=1)
+    assert (res[:, 0] * bnorm <= 2e-10).all() and (res_gpu[:, 0] * bnorm <= 2e-10).all()  # absolute 1e-10 seed test
+    assert (np.abs(res_gpu - res) <= 1e-2 * res + 1e-9).all(), np.abs(res_gpu - res).max()
+    ok = res <= 1e-8
     err = np.linalg.norm(x - xo, axis=2) / np.linalg.norm(xo, axis=2)
-    assert err[ok].max() < 1e-7, err[ok].max()
+    assert err[ok].max() < 1e-5, err[ok].max()
