@@ -338,8 +338,8 @@ def w_error_imag_axis():
     x64, e64, _ = sg.solve_batch(op, bb, sh, threshold=THRESHOLD)
     xm, em, _ = sg.solve_batch(op, bb, sh, threshold=THRESHOLD, precision=1)
     v = linter.coulomb_v(s)
-    W64 = linter.w_from_chi(linter.chi_matrix(op, bb, x64, nocc, f), v)
-    WM = linter.w_from_chi(linter.chi_matrix(op, bb, xm, nocc, f), v)
+    W64 = linter.w_from_chi(op, linter.chi_matrix(op, bb, x64, nocc, f), v)
+    WM = linter.w_from_chi(op, linter.chi_matrix(op, bb, xm, nocc, f), v)
     d = WM - W64
     norm = float(np.max(np.linalg.norm(d, axis=(1, 2)) / np.linalg.norm(W64, axis=(1, 2))))
     big = np.abs(W64) >= 1e-3 * np.abs(W64).max(axis=(1, 2), keepdims=True)

@@ -302,6 +302,34 @@ typedef struct sgw_chi_desc {
 
 sgw_status sgw_chi(sgw_operator* op, const sgw_chi_desc* desc);
 
+/* Screened Coulomb interaction on the perturbation set from the density
+ * response of sgw_chi, for every frequency f:
+ *   eps_f = 1 - diag(v) chi_f,  W_f = eps_f^-1 diag(v)   (RPA: Hartree only)
+ * with chi_f[p][q] = chi[(q*nfreq + f)*ldc + p] as sgw_chi writes it and
+ * v[p] = v(q+G_p) (Ry).  Replaces invert_epsilon (invert_epsilon.f90:59-66,
+ * ZGETRF + ZGETRI per frequency) and coulpade (coulpade.f90, the scaling by
+ * the Coulomb kernel), fed by the dielectric columns of coulomb.f90:146-157
+ * and the Hartree response of dv_of_drho (solve_linter.f90:556).  Outputs in
+ * the reference's array layout scrcoul_g(ig, igp, f) (Fortran order, offset
+ * ig + npert*(igp + npert*f); unfold_w.f90 stores conjugates):
+ *   inveps(ig, igp, f) = conj(eps_f^-1[igp][ig])            (invert_epsilon)
+ *   w(ig, igp, f)      = inveps(ig, igp, f) * v[ig]          (coulpade)
+ * Either output may be NULL.  FP64 Gauss-Jordan with partial pivoting, one
+ * CTA per frequency.  A singular matrix returns SGW_NAN (the reference
+ * aborts).  memory 0 host, 1 device. */
+typedef struct sgw_w_desc {
+  int32_t npert;
+  int32_t nfreq;
+  const sgw_zcomplex* chi;
+  int64_t ldc;
+  const double* vcoul;
+  sgw_zcomplex* inveps;
+  sgw_zcomplex* w;
+  int32_t memory;
+} sgw_w_desc;
+
+sgw_status sgw_screened_coulomb(sgw_operator* op, const sgw_w_desc* desc);
+
 /* The Green's function of one k-point (green_function, green.f90:105-226):
  * for every G' point igp of the correlation mesh with ig = ig_of_gp[igp] != 0,
  * solve (H - omega) x = -delta_{G, ig} for all omega at once (green.f90:199-207,
@@ -478,7 +506,8 @@ sgw_status sgw_last_timing(sgw_operator* op, double* ms, int64_t* launches);
  * (mixed precision); kernel 3 = the last sgw_coulomb_rhs (both of its
  * kernels), 4 = the last sgw_chi, 5 = the last sgw_vjp; 6 = the host-to-device
  * and 7 = the device-to-host copies of the last host-memory sgw_solve_batch
- * (0 after a device-memory call). */
+ * (0 after a device-memory call); 8 = the last sgw_screened_coulomb, 9 = the
+ * last sgw_sigma_diag. */
 sgw_status sgw_kernel_timing(sgw_operator* op, int32_t kernel, double* ms, int64_t* launches);
 
 /* One-line description of the last error on this thread. */

@@ -91,3 +91,12 @@ def green_function(ops, npw, ig_of_gp, gmap, omega, threshold=1e-10, lmax=4):
         for f in range(om.size):
             out[f, p, ok] = x[r, f, gm[ok] - 1]
     return out, int(ierr.max())
+
+
+def w_from_chi(chi, v):
+    """W(omega) = (1 - v chi)^-1 v (invert_epsilon.f90:59-66 inverse, coulpade.f90 scaling by the
+    Coulomb kernel, RPA) by dense LU solves: chi (nfreq, P, P) with chi[f, p, q] the response
+    component p of perturbation q."""
+    eye = np.eye(chi.shape[-1])
+    eps = eye[None] - np.asarray(v)[None, :, None] * chi
+    return np.linalg.solve(eps, np.broadcast_to(np.diag(v), eps.shape))

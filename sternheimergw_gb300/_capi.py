@@ -80,6 +80,11 @@ class TuneResult(C.Structure):
                 ("us_per_apply", C.c_double), ("candidates", C.c_int32), ("cached", C.c_int32)]
 
 
+class WDesc(C.Structure):
+    _fields_ = [("npert", C.c_int32), ("nfreq", C.c_int32), ("chi", C.c_void_p), ("ldc", C.c_int64),
+                ("vcoul", C.c_void_p), ("inveps", C.c_void_p), ("w", C.c_void_p), ("memory", C.c_int32)]
+
+
 class GreenDesc(C.Structure):
     _fields_ = [("num_gp", C.c_int32), ("ig_of_gp", C.c_void_p), ("num_g_corr", C.c_int32), ("map", C.c_void_p),
                 ("num_freq", C.c_int32), ("omega", C.c_void_p), ("lmax", C.c_int32), ("max_iter", C.c_int32),
@@ -110,6 +115,7 @@ SIGNATURES = [
     ("sgw_coulomb_rhs", C.c_int, [C.c_void_p, C.POINTER(RhsDesc)]),
     ("sgw_chi", C.c_int, [C.c_void_p, C.POINTER(ChiDesc)]),
     ("sgw_green_function", C.c_int, [C.c_void_p, C.POINTER(GreenDesc)]),
+    ("sgw_screened_coulomb", C.c_int, [C.c_void_p, C.POINTER(WDesc)]),
     ("sgw_operator_set_vloc", C.c_int, [C.c_void_p, C.c_void_p, C.c_int64]),
     ("sgw_solve_adjoint", C.c_int, [C.c_void_p, C.POINTER(AdjointDesc)]),
     ("sgw_vjp", C.c_int, [C.c_void_p, C.POINTER(VjpDesc)]),

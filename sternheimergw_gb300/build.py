@@ -17,7 +17,7 @@ CSRC = os.path.join(HERE, "csrc")
 INCLUDE = os.path.join(ROOT, "include")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libsgw_gb300.so")
-UNITS = ["capi.cu", "k_f64.cu", "k_f32.cu", "mixed.cu", "refine.cu", "noalloc.cu", "linter.cu", "multi.cu"]
+UNITS = ["capi.cu", "k_f64.cu", "k_f32.cu", "mixed.cu", "refine.cu", "noalloc.cu", "linter.cu", "screen.cu", "multi.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I", INCLUDE]
 

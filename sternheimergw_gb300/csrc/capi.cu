@@ -789,7 +789,8 @@ sgw_status sgw_operator_destroy(sgw_operator* op) {
                     &op->ws32.vec, &op->ws32.coef, &op->ws32.col, &op->ws32.counter, &op->st_bb, &op->st_sigma,
                     &op->st_xx, &op->st_ierr, &op->st_iters, &op->st_misc, &op->st_misc2, &op->st_misc3,
                     &op->st_ref, &op->st_ref2, &op->st_resid, &op->nlkq, &op->lt_psi, &op->lt_box, &op->lt_nlk, &op->lt_evc, &op->lt_dv, &op->lt_bb,
-                    &op->lt_flag, &op->lt_part, &op->lt_sidx, &op->lt_xx, &op->lt_chi};
+                    &op->lt_flag, &op->lt_part, &op->lt_sidx, &op->lt_xx, &op->lt_chi, &op->lt_w,
+                    &op->lt_wwork, &op->lt_sig};
   for (DevBuf* b : bufs) b->release();
   for (int i = 0; i < 2 * kMaxTimedLaunches; ++i)
     if (op->kev[i]) cudaEventDestroy(op->kev[i]);
@@ -814,7 +815,7 @@ sgw_status sgw_operator_trim(sgw_operator* op) {
                     &op->st_iters, &op->st_misc, &op->st_misc2, &op->st_misc3, &op->st_ref, &op->st_ref2,
                     &op->st_resid, &op->lt_psi, &op->lt_box,
                     &op->lt_nlk, &op->lt_evc, &op->lt_dv, &op->lt_bb, &op->lt_flag, &op->lt_part, &op->lt_sidx,
-                    &op->lt_xx, &op->lt_chi};
+                    &op->lt_xx, &op->lt_chi, &op->lt_w, &op->lt_wwork, &op->lt_sig};
   for (DevBuf* b : bufs) b->release();
   return SGW_OK;
 }

@@ -97,7 +97,9 @@ enum KernelKind {
   K_VJP = 5,
   K_COPY_IN = 6,
   K_COPY_OUT = 7,
-  K_NUM = 8
+  K_SCREEN = 8,
+  K_SIGMA = 9,
+  K_NUM = 10
 };
 constexpr int kMaxTimedLaunches = 64;
 
@@ -141,6 +143,8 @@ struct sgw_operator {
   sgw::DevBuf st_ref, st_ref2, st_resid;  // restart rounds and warm starts (sgw_solve_batch_ex)
   // right-hand-side build and chi accumulation
   sgw::DevBuf lt_psi, lt_box, lt_nlk, lt_evc, lt_dv, lt_bb, lt_flag, lt_part, lt_sidx, lt_xx, lt_chi;
+  // screened Coulomb interaction and self-energy
+  sgw::DevBuf lt_w, lt_wwork, lt_sig;
 };
 
 namespace sgw {

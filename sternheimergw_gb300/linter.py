@@ -17,7 +17,8 @@
   * green_rhs / green_shifts   b = -delta_{G,G'} with shifts -omega
                   (green.f90:195-207, freqbins.f90:302-323);
   * coulomb_v / w_from_chi     v = 8 pi / (Omega |q+G|^2) and
-                  W = (1 - v chi)^-1 v (invert_epsilon.f90:23-90).
+                  W = (1 - v chi)^-1 v on the GPU (sgw_screened_coulomb:
+                  invert_epsilon.f90:23-90 and coulpade.f90).
 """
 from __future__ import annotations
 
@@ -133,14 +134,12 @@ def coulomb_v(system):
     return 8 * math.pi / (system["omega"] * np.sum(qg ** 2, 1))
 
 
-def w_from_chi(chi, v):
-    """W(omega) = (1 - v chi)^-1 v on the perturbation set (invert_epsilon.f90:23-90, coulpade.f90)."""
+def w_from_chi(op, chi, v):
+    """W(omega) = (1 - v chi)^-1 v on the perturbation set, on the GPU (sgw_screened_coulomb;
+    invert_epsilon.f90:23-90, coulpade.f90).  chi: (nfreq, P, P) from chi_matrix (numpy or CUDA
+    torch); returns W[f, p, q] (the reference's arrays hold the conjugate transpose)."""
     if type(chi).__module__.startswith("torch"):
-        import torch
-        vv = torch.as_tensor(v, dtype=chi.dtype, device=chi.device)
-        eye = torch.eye(chi.shape[-1], dtype=chi.dtype, device=chi.device)
-        eps = eye[None] - vv[None, :, None] * chi
-        return torch.linalg.solve(eps, torch.diag(vv)[None].expand_as(eps))
-    eye = np.eye(chi.shape[-1])
-    eps = eye[None] - v[None, :, None] * chi
-    return np.linalg.solve(eps, np.broadcast_to(np.diag(v), eps.shape))
+        raw = chi.permute(2, 0, 1).contiguous()
+        return solver.screened_coulomb(op, raw, v).conj().resolve_conj()
+    raw = np.ascontiguousarray(np.transpose(chi, (2, 0, 1)))
+    return np.conj(solver.screened_coulomb(op, raw, v))

@@ -429,6 +429,40 @@ def chi(AA: _Operator, bb, xx, nbnd, shift_plus, shift_minus, weight=1.0):
     return out
 
 
+def screened_coulomb(AA: _Operator, chi_raw, vcoul, want_inveps=False):
+    """W on the perturbation set from sgw_chi's output (sgw_screened_coulomb: invert_epsilon.f90:59-66
+    and coulpade.f90 on eps = 1 - v chi, RPA).
+
+    chi_raw: (Q, nfreq, P) as solver.chi returns it (numpy or CUDA torch); vcoul: (P,) v(q+G).
+    Returns w (and inveps with want_inveps), each (nfreq, P, P) with w[f, igp, ig] =
+    W(ig, igp, f) of the reference's Fortran array scrcoul_g."""
+    d = _capi.WDesc()
+    Q, F, P = chi_raw.shape
+    if Q != P:
+        raise ValueError("the dielectric matrix needs every perturbation as a response component (Q = P)")
+    if _is_torch(chi_raw):
+        import torch
+        chi_raw = chi_raw.contiguous()
+        v = torch.as_tensor(np.asarray(vcoul, dtype=np.float64), device=chi_raw.device)
+        w = torch.empty((F, P, P), dtype=torch.complex128, device=chi_raw.device)
+        ie = torch.empty_like(w) if want_inveps else None
+        _order_after_torch(AA)
+        d.memory = 1
+        d.chi, d.vcoul, d.w = chi_raw.data_ptr(), v.data_ptr(), w.data_ptr()
+        d.inveps = ie.data_ptr() if ie is not None else None
+    else:
+        chi_raw = _c128(chi_raw)
+        v = np.ascontiguousarray(vcoul, dtype=np.float64)
+        w = np.empty((F, P, P), dtype=np.complex128)
+        ie = np.empty_like(w) if want_inveps else None
+        d.memory = 0
+        d.chi, d.vcoul, d.w = chi_raw.ctypes.data, v.ctypes.data, w.ctypes.data
+        d.inveps = ie.ctypes.data if ie is not None else None
+    d.npert, d.nfreq, d.ldc = P, F, P
+    _capi.check(_capi.lib().sgw_screened_coulomb(AA.handle, C.byref(d)), "sgw_screened_coulomb")
+    return (w, ie) if want_inveps else w
+
+
 def solve_adjoint(AA: _Operator, gbar, sigma, *, lmax=4, threshold=1e-10, max_iter=10000, precision=0,
                   checkpoint_iters=8):
     """lambda_rs = A(sigma_rs)^-H gbar_rs: the Hermitian-conjugate systems at conj(sigma), one

@@ -220,8 +220,8 @@ def test_mixed_w_error_c4(gpu_lib):
     xm, em, _ = sg.solve_batch(op, bb, sh, threshold=1e-10, precision=1)
     assert (e64 == 0).all() and (em == 0).all()
     v = linter.coulomb_v(s)
-    W64 = linter.w_from_chi(linter.chi_matrix(op, bb, x64, nocc, f), v)
-    WM = linter.w_from_chi(linter.chi_matrix(op, bb, xm, nocc, f), v)
+    W64 = linter.w_from_chi(op, linter.chi_matrix(op, bb, x64, nocc, f), v)
+    WM = linter.w_from_chi(op, linter.chi_matrix(op, bb, xm, nocc, f), v)
     err = np.linalg.norm(WM - W64, axis=(1, 2)) / np.linalg.norm(W64, axis=(1, 2))
     assert err.max() < 1e-6, err.max()
 
