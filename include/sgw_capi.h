@@ -330,6 +330,37 @@ typedef struct sgw_w_desc {
 
 sgw_status sgw_screened_coulomb(sgw_operator* op, const sgw_w_desc* desc);
 
+/* Diagonal correlation self-energy matrix elements on the imaginary axis
+ * (sigma_correlation, sigma.f90:528-750, with the G*W product of sigma_prod
+ * :480-525 and the <psi_n|Sigma|psi_n> contraction of sigma_expect.f90),
+ * evaluated at the chemical potential mu from a Green's function solved on
+ * the right-hand sides u_(n,G) = psi_n shifted by G (the Sternheimer form of
+ * the G*W product: no real-space sextic FFT):
+ *   sigma[n] = alpha sum_j weight[j] sum_(G1,G2) Wc_j(G1,G2) pair_n(G1,G2,j)
+ *   Wc_j = W_j - diag(vcoul)         (correlation part of W at i y_j)
+ *   pair_n(G1,G2,j) = <u_(n,G1)| G(mu + i y_j) + G(mu - i y_j) |u_(n,G2)>
+ * with W in sgw_screened_coulomb's layout (w[(j*P + igp)*P + ig] =
+ * W(ig, igp, j) of the reference's array: W_j(G1, G2) = conj(w[(j*P+G1)*P+G2]))
+ * and pair in sgw_chi's layout per band, pair[n*ldp + (G2*nfreq + j)*P + G1]
+ * (sgw_chi with bra u_(n,G1), solutions of the Green's-function systems
+ * (H - omega) y = -u_(n,G2) at omega = mu +- i y_j, weight -2 and the
+ * +-i y_j shift pairs).  memory 0 host, 1 device. */
+typedef struct sgw_sigma_desc {
+  int32_t nbnd;
+  int32_t npert;
+  int32_t nfreq;
+  const sgw_zcomplex* pair;
+  int64_t ldp;
+  const sgw_zcomplex* w;
+  const double* vcoul;
+  const double* weight;
+  sgw_zcomplex alpha;
+  sgw_zcomplex* sigma;
+  int32_t memory;
+} sgw_sigma_desc;
+
+sgw_status sgw_sigma_diag(sgw_operator* op, const sgw_sigma_desc* desc);
+
 /* The Green's function of one k-point (green_function, green.f90:105-226):
  * for every G' point igp of the correlation mesh with ig = ig_of_gp[igp] != 0,
  * solve (H - omega) x = -delta_{G, ig} for all omega at once (green.f90:199-207,

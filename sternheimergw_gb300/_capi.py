@@ -85,6 +85,12 @@ class WDesc(C.Structure):
                 ("vcoul", C.c_void_p), ("inveps", C.c_void_p), ("w", C.c_void_p), ("memory", C.c_int32)]
 
 
+class SigmaDesc(C.Structure):
+    _fields_ = [("nbnd", C.c_int32), ("npert", C.c_int32), ("nfreq", C.c_int32), ("pair", C.c_void_p),
+                ("ldp", C.c_int64), ("w", C.c_void_p), ("vcoul", C.c_void_p), ("weight", C.c_void_p),
+                ("alpha", ZComplex), ("sigma", C.c_void_p), ("memory", C.c_int32)]
+
+
 class GreenDesc(C.Structure):
     _fields_ = [("num_gp", C.c_int32), ("ig_of_gp", C.c_void_p), ("num_g_corr", C.c_int32), ("map", C.c_void_p),
                 ("num_freq", C.c_int32), ("omega", C.c_void_p), ("lmax", C.c_int32), ("max_iter", C.c_int32),
@@ -116,6 +122,7 @@ SIGNATURES = [
     ("sgw_chi", C.c_int, [C.c_void_p, C.POINTER(ChiDesc)]),
     ("sgw_green_function", C.c_int, [C.c_void_p, C.POINTER(GreenDesc)]),
     ("sgw_screened_coulomb", C.c_int, [C.c_void_p, C.POINTER(WDesc)]),
+    ("sgw_sigma_diag", C.c_int, [C.c_void_p, C.POINTER(SigmaDesc)]),
     ("sgw_operator_set_vloc", C.c_int, [C.c_void_p, C.c_void_p, C.c_int64]),
     ("sgw_solve_adjoint", C.c_int, [C.c_void_p, C.POINTER(AdjointDesc)]),
     ("sgw_vjp", C.c_int, [C.c_void_p, C.POINTER(VjpDesc)]),

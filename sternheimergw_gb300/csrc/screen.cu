@@ -175,14 +175,16 @@ sgw_status screened_coulomb(sgw_operator* op, const sgw_w_desc* d) {
   }
   sgw_status s;
   // staging: [chi (host form) | v | inveps | w | flag] and the global matrices when they do not fit
-  const size_t chi_b = sizeof(zcd) * (size_t)F * P * P;
-  if ((s = op->lt_w.ensure(chi_b + sizeof(double) * P + 2 * sizeof(zcd) * F * PP + 256)) != SGW_OK) return s;
+  auto al = [](size_t v) { return (v + 255) / 256 * 256; };
+  const size_t chi_b = al(sizeof(zcd) * (size_t)F * P * P), v_b = al(sizeof(double) * P);
+  const size_t m_b = al(sizeof(zcd) * F * PP);
+  if ((s = op->lt_w.ensure(chi_b + v_b + 2 * m_b + 256)) != SGW_OK) return s;
   unsigned char* base = reinterpret_cast<unsigned char*>(op->lt_w.p);
   zcd* chi_d = reinterpret_cast<zcd*>(base);
   double* v_d = reinterpret_cast<double*>(base + chi_b);
-  zcd* ie_d = reinterpret_cast<zcd*>(base + chi_b + sizeof(double) * P);
-  zcd* w_d = ie_d + F * PP;
-  int* flag = reinterpret_cast<int*>(w_d + F * PP);
+  zcd* ie_d = reinterpret_cast<zcd*>(base + chi_b + v_b);
+  zcd* w_d = reinterpret_cast<zcd*>(base + chi_b + v_b + m_b);
+  int* flag = reinterpret_cast<int*>(base + chi_b + v_b + 2 * m_b);
   zcd* work = nullptr;
   if (!in_smem) {
     if ((s = op->lt_wwork.ensure(sizeof(zcd) * F * PP)) != SGW_OK) return s;
@@ -233,8 +235,99 @@ sgw_status screened_coulomb(sgw_operator* op, const sgw_w_desc* d) {
   return SGW_OK;
 }
 
+// sigma[n] = alpha sum_j weight_j sum_(G1, G2) Wc_j(G1, G2) pair_n[(G2 nfreq + j) P + G1],
+// Wc_j = W_j - diag(v), W_j(G1, G2) = conj(w[(j P + G1) P + G2]); one CTA per band,
+// partial sums in a fixed order (deterministic).
+__global__ void sigma_diag_kernel(int nbnd, int P, int N, const zcd* pair, long long ldp, const zcd* w,
+                                  const double* v, const double* weight, zcd alpha, zcd* sigma) {
+  __shared__ zcd red[32];
+  const int n = blockIdx.x;
+  if (n >= nbnd) return;
+  const long long tot = (long long)N * P * P;
+  const zcd* pr = pair + (size_t)n * ldp;
+  zcd acc = {0.0, 0.0};
+  for (long long e = threadIdx.x; e < tot; e += blockDim.x) {
+    const int g1 = (int)(e % P);
+    const long long t = e / P;
+    const int j = (int)(t % N), g2 = (int)(t / N);
+    zcd wc = conj(w[((size_t)j * P + g1) * P + g2]);
+    if (g1 == g2) wc.re -= v[g1];
+    acc += weight[j] * (wc * pr[e]);
+  }
+  const zcd sum = cta_sum(acc, red);
+  if (threadIdx.x == 0) sigma[n] = alpha * sum;
+}
+
+sgw_status sigma_diag(sgw_operator* op, const sgw_sigma_desc* d) {
+  if (!op || !d) {
+    set_error("null argument");
+    return SGW_ERR_ARG;
+  }
+  const int nb = d->nbnd, P = d->npert, N = d->nfreq;
+  if (nb < 0 || P < 0 || N < 0 || d->memory < 0 || d->memory > 1) {
+    set_error("invalid self-energy description");
+    return SGW_ERR_ARG;
+  }
+  if (nb == 0) return SGW_OK;
+  if (P == 0 || N == 0 || !d->pair || !d->w || !d->vcoul || !d->weight || !d->sigma ||
+      d->ldp < (long long)N * P * P) {
+    set_error("null self-energy array or band stride too small");
+    return SGW_ERR_ARG;
+  }
+  const size_t PP = (size_t)P * P;
+  auto al = [](size_t v) { return (v + 255) / 256 * 256; };
+  const size_t pair_b = al(sizeof(zcd) * nb * (size_t)N * PP), w_b = al(sizeof(zcd) * N * PP);
+  const size_t v_b = al(sizeof(double) * P), wt_b = al(sizeof(double) * N);
+  sgw_status s;
+  if ((s = op->lt_sig.ensure(pair_b + w_b + v_b + wt_b + al(sizeof(zcd) * nb))) != SGW_OK) return s;
+  unsigned char* base = reinterpret_cast<unsigned char*>(op->lt_sig.p);
+  zcd* pair_d = reinterpret_cast<zcd*>(base);
+  zcd* w_d = reinterpret_cast<zcd*>(base + pair_b);
+  double* v_d = reinterpret_cast<double*>(base + pair_b + w_b);
+  double* wt_d = reinterpret_cast<double*>(base + pair_b + w_b + v_b);
+  zcd* sig_d = reinterpret_cast<zcd*>(base + pair_b + w_b + v_b + wt_b);
+  const cudaMemcpyKind kind = d->memory ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+  SGW_CK(cudaEventRecord(op->lev0, op->stream));
+  const zcd* pair_in = reinterpret_cast<const zcd*>(d->pair);
+  const zcd* w_in = reinterpret_cast<const zcd*>(d->w);
+  long long ldp = d->ldp;
+  if (d->memory == 0) {
+    SGW_CK(cudaMemcpy2DAsync(pair_d, sizeof(zcd) * N * PP, d->pair, sizeof(zcd) * d->ldp, sizeof(zcd) * N * PP, nb,
+                             cudaMemcpyHostToDevice, op->stream));
+    SGW_CK(cudaMemcpyAsync(w_d, d->w, w_b, cudaMemcpyHostToDevice, op->stream));
+    pair_in = pair_d;
+    w_in = w_d;
+    ldp = (long long)N * PP;
+  }
+  SGW_CK(cudaMemcpyAsync(v_d, d->vcoul, sizeof(double) * P, kind, op->stream));
+  SGW_CK(cudaMemcpyAsync(wt_d, d->weight, sizeof(double) * N, kind, op->stream));
+  zcd* out = d->memory ? reinterpret_cast<zcd*>(d->sigma) : sig_d;
+  sigma_diag_kernel<<<nb, 256, 0, op->stream>>>(nb, P, N, pair_in, ldp, w_in, v_d, wt_d, zcd{d->alpha.re, d->alpha.im},
+                                                 out);
+  SGW_CK(cudaGetLastError());
+  if (d->memory == 0) SGW_CK(cudaMemcpyAsync(d->sigma, sig_d, sizeof(zcd) * nb, cudaMemcpyDeviceToHost, op->stream));
+  SGW_CK(cudaEventRecord(op->lev1, op->stream));
+  SGW_CK(cudaStreamSynchronize(op->stream));
+  float ms = 0.f;
+  SGW_CK(cudaEventElapsedTime(&ms, op->lev0, op->lev1));
+  op->kernel_ms[K_SIGMA] = ms;
+  op->kernel_launches[K_SIGMA] = 1;
+  return SGW_OK;
+}
+
 }  // namespace
 }  // namespace sgw
+
+extern "C" sgw_status sgw_sigma_diag(sgw_operator* op, const sgw_sigma_desc* desc) {
+  try {
+    sgw::CallScope cs(op);
+    if (cs.status() != SGW_OK) return cs.status();
+    return sgw::sigma_diag(op, desc);
+  } catch (...) {
+    sgw::set_error("host exception in sgw_sigma_diag");
+    return SGW_ERR_NOMEM;
+  }
+}
 
 extern "C" sgw_status sgw_screened_coulomb(sgw_operator* op, const sgw_w_desc* desc) {
   try {

@@ -304,3 +304,14 @@ def config(name: str, seed: int | None = None):
         x = np.sort(rng.uniform(-30.0, 30.0, 35))
         return s, (x + 0.1j) / RY_EV
     raise ValueError(name)
+
+
+def midgap(system):
+    """Chemical potential in the gap of the k+q Hamiltonian (where the Green's
+    function is evaluated): the midpoint between its nocc-th and (nocc+1)-th
+    eigenvalues (dense FP64 eigvalsh; small systems)."""
+    nr = [int(v) for v in system["nr"]]
+    h = dense_h(system["mill"], system["g2kin"], system["vrs"], nr, system["vkb"], system["dvan"])
+    w = np.linalg.eigvalsh(h)
+    n = int(system["nocc"])
+    return 0.5 * float(w[n - 1] + w[n])
