@@ -18,7 +18,9 @@
                   (green.f90:195-207, freqbins.f90:302-323);
   * coulomb_v / w_from_chi     v = 8 pi / (Omega |q+G|^2) and
                   W = (1 - v chi)^-1 v on the GPU (sgw_screened_coulomb:
-                  invert_epsilon.f90:23-90 and coulpade.f90).
+                  invert_epsilon.f90:23-90 and coulpade.f90);
+  * iterative_w   the self-consistent screening loop (solve_linter.f90:280-575)
+                  with Broyden mixing (mix_pot_c.f90) and warm-started solves.
 """
 from __future__ import annotations
 
@@ -26,7 +28,7 @@ import math
 
 import numpy as np
 
-from . import solver, synth
+from . import mixing, solver, synth
 
 
 def dvbare_all(system, perts=None):
@@ -143,3 +145,95 @@ def w_from_chi(op, chi, v):
         return solver.screened_coulomb(op, raw, v).conj().resolve_conj()
     raw = np.ascontiguousarray(np.transpose(chi, (2, 0, 1)))
     return np.conj(solver.screened_coulomb(op, raw, v))
+
+
+def iterative_w(op, system, freq, *, alpha_mix=0.7, nmix=4, tr2=1e-20, niter=40, threshold=1e-10, lmax=4,
+                precision=0, warm_start=True, first_threshold=1e-2):
+    """Self-consistent screening on the perturbation set: the iterative path of
+    solve_linter (solve_linter.f90:280-575) with Broyden mixing of the induced
+    potential (mix_pot_c.f90), on the GPU.
+
+    For every perturbation q the induced potential is kept as its coefficients
+    c[q, f, :] on the perturbation set (the set on which the direct method
+    forms eps), so the right-hand side of band v at frequency f is
+    B^T (e_q + c[q, f]) with B the bare right-hand sides (sgw_coulomb_rhs;
+    dvqpsi_us + apply_dpot + orthogonalize, :395-409).  Iteration 1 solves the
+    bare right-hand sides for all frequencies in one multishift call (:329-379);
+    later iterations solve each (q, f, v) for +-omega_f (:381-458), with the
+    threshold min(0.1 sqrt(dr2), 1e-2) (:425) and, with warm_start, the
+    previous iteration's solutions as starting guesses (the restart the
+    reference disables at :411-414).  The Hartree response v * Delta rho
+    (dv_of_drho, :556; sgw_chi for Delta rho on the set) is mixed per
+    perturbation until dr2 < tr2 * nfreq (:566).  At convergence e_q + c is
+    column q of eps^-1 (the reference's iterative output, :596-604) and
+    W = eps^-1 v.
+
+    Returns (W[f, p, q], info) with info: iterations, operator applies per
+    iteration (sum of outer iterations x 2 lmax), the dr2 history."""
+    import torch
+
+    nocc = int(system["nocc"])
+    P = len(system["gpert"])
+    F = len(freq)
+    v = coulomb_v(system)
+    B = coulomb_rhs(op, system, device=True)                       # (P * nocc, n)
+    n = B.shape[1]
+    B3 = B.reshape(P, nocc * n)
+    et = np.asarray(system["et"])
+    freq = np.asarray(freq, dtype=np.complex128)
+    plus, minus = pm_pairs(freq)
+    mixers = [mixing.BroydenMixer(nmix) for _ in range(P)]
+    c = np.zeros((P, F, P), dtype=np.complex128)
+    active = list(range(P))
+    x_prev = None
+    prev_cols = None
+    hist, applies = [], []
+    thresh = first_threshold
+    for it in range(1, niter + 1):
+        if it == 1:
+            # every frequency at once on the bare right-hand sides (the multishift first iteration)
+            sh = torch.from_numpy(np.tile(coulomb_shifts(system, freq), (P, 1))).cuda()
+            x, ierr, iters = solver.solve_batch(op, B, sh, lmax=lmax, threshold=thresh, precision=precision)
+            chi = solver.chi(op, B, x, nocc, plus, minus)                # (P[q], F, P[p'])
+            drho = chi.cpu().numpy()
+            applies.append(int(iters.sum().item()) * 2 * lmax)
+        else:
+            cols = active
+            coef = np.zeros((len(cols), F, P), dtype=np.complex128)
+            for i, q in enumerate(cols):
+                coef[i] = c[q]
+                coef[i, :, q] += 1.0
+            ct = torch.from_numpy(coef.reshape(len(cols) * F, P)).cuda()
+            rhs = (ct @ B3).reshape(len(cols) * F * nocc, n).contiguous()
+            om = freq[None, :, None]
+            e = et[None, None, :]
+            sig = np.stack([-(e + om), -(e - om)], -1) * np.ones((len(cols), 1, 1, 1))
+            sh = torch.from_numpy(np.ascontiguousarray(sig.reshape(len(cols) * F * nocc, 2))).cuda()
+            x0 = None
+            if warm_start and x_prev is not None and prev_cols is not None:
+                keep = [prev_cols.index(q) for q in cols]
+                x0 = x_prev.reshape(len(prev_cols), F * nocc, 2, n)[keep].reshape(len(cols) * F * nocc, 2, n)
+            x, ierr, iters = solver.solve_batch(op, rhs, sh, lmax=lmax, threshold=thresh, precision=precision, x0=x0)
+            raw = solver.chi(op, B, x, nocc, np.array([0], np.int32), np.array([1], np.int32))  # (cols*F, 1, P)
+            drho = np.zeros((P, F, P), dtype=np.complex128)
+            drho[cols] = raw.cpu().numpy().reshape(len(cols), F, P)
+            applies.append(int(iters.sum().item()) * 2 * lmax)
+            x_prev, prev_cols = x, list(cols)
+        worst = 0.0
+        still = []
+        for q in active:
+            vout = v[None, :] * drho[q]                                # Hartree response, (F, P)
+            new, dr2, conv = mixers[q].mix(vout, c[q], alpha_mix, tr2 * F)
+            worst = max(worst, dr2)
+            if not conv:
+                c[q] = new.reshape(F, P)
+                still.append(q)
+        hist.append(worst)
+        active = still
+        if not active:
+            break
+        thresh = min(0.1 * np.sqrt(worst), 1e-2)
+        thresh = max(thresh, threshold)
+    inveps = np.transpose(c, (1, 2, 0)) + np.eye(P)[None]             # [f, p', q]
+    W = inveps * v[None, None, :]
+    return W, dict(iterations=len(hist), converged=not active, dr2=hist, applies=applies)
