@@ -147,7 +147,7 @@ def w_from_chi(op, chi, v):
     return np.conj(solver.screened_coulomb(op, raw, v))
 
 
-def iterative_w(op, system, freq, *, alpha_mix=0.7, nmix=4, tr2=1e-20, niter=40, threshold=1e-10, lmax=4,
+def iterative_w(op, system, freq, *, alpha_mix=0.7, nmix=4, tr2=1e-18, niter=80, threshold=1e-10, lmax=4,
                 precision=0, warm_start=True, first_threshold=1e-2):
     """Self-consistent screening on the perturbation set: the iterative path of
     solve_linter (solve_linter.f90:280-575) with Broyden mixing of the induced
