@@ -685,7 +685,7 @@ def run_gpu(args, rank, world):
         link[name] = x_h.nbytes / (e0.elapsed_time(e1) * 1e-3) / 1e9
     del xt
     e2e = {}
-    for prec, key, frac in ((1, "mixed", fracm), (0, "fp64", frac64)):
+    for prec, key, frac in ((1, "mixed", frac_value), (0, "fp64", frac64)):
         e2e_ms, copy_ms = [], []
         for k in range(max(1, min(args.steps, 3))):
             flush_l2(l2)

@@ -4,8 +4,9 @@ Reads algo/linear_solver/test/lin_prob.xml.bz2 from the reference tree (an
 iotk binary file: Fortran sequential records, each data record carrying a
 4-byte prefix before its payload) and stores DIMENSION, LIST_SHIFT,
 LINEAR_OPERATOR (column-major n x n) and RIGHT_HAND_SIDE.  The solver test
-(linear_solver.pf:125-345) reads the same four items.  Run once, here:
-    python tests/golden/make_lin_prob.py /root/reference
+(linear_solver.pf:125-345) reads the same four items.  Run once, with the
+path of a reference checkout:
+    python tests/golden/make_lin_prob.py <reference checkout>
 """
 import bz2
 import os
@@ -47,4 +48,6 @@ def main(ref_root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: make_lin_prob.py <reference checkout>")
+    main(sys.argv[1])
