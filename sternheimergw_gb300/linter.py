@@ -160,9 +160,10 @@ def iterative_w(op, system, freq, *, alpha_mix=0.7, nmix=4, tr2=1e-18, niter=80,
     dvqpsi_us + apply_dpot + orthogonalize, :395-409).  Iteration 1 solves the
     bare right-hand sides for all frequencies in one multishift call (:329-379);
     later iterations solve each (q, f, v) for +-omega_f (:381-458), with the
-    threshold min(0.1 sqrt(dr2), 1e-2) (:425) and, with warm_start, the
+    threshold min(0.1 sqrt(dr2), 1e-2) (:425), or - with warm_start - the
     previous iteration's solutions as starting guesses (the restart the
-    reference disables at :411-414).  The Hartree response v * Delta rho
+    reference disables at :411-414) and the final threshold (a warm start
+    keeps the errors of the solutions it starts from).  The Hartree response v * Delta rho
     (dv_of_drho, :556; sgw_chi for Delta rho on the set) is mixed per
     perturbation until dr2 < tr2 * nfreq (:566).  At convergence e_q + c is
     column q of eps^-1 (the reference's iterative output, :596-604) and
@@ -232,8 +233,13 @@ def iterative_w(op, system, freq, *, alpha_mix=0.7, nmix=4, tr2=1e-18, niter=80,
         active = still
         if not active:
             break
-        thresh = min(0.1 * np.sqrt(worst), 1e-2)
-        thresh = max(thresh, threshold)
+        if warm_start:
+            # a warm start carries every earlier error of the solutions forward, so the
+            # per-frequency solves that later iterations start from are solved to the
+            # final threshold; their corrections shrink with the mixing residual
+            thresh = threshold
+        else:
+            thresh = max(min(0.1 * np.sqrt(worst), 1e-2), threshold)
     inveps = np.transpose(c, (1, 2, 0)) + np.eye(P)[None]             # [f, p', q]
     W = inveps * v[None, None, :]
     return W, dict(iterations=len(hist), converged=not active, dr2=hist, applies=applies)
