@@ -158,20 +158,6 @@ CallScope::~CallScope() {
   if (dev_ >= 0 && prev_ >= 0) cudaSetDevice(prev_);
 }
 
-sgw_status finish_call(sgw_operator* op, sgw_status s) {
-  if (s < 0 || !op || !op->opflag.p) return s;
-  int flag = 0;
-  if (cudaMemcpy(&flag, op->opflag.p, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) {
-    set_error("reading the operator's error flag failed");
-    return SGW_ERR_CUDA;
-  }
-  if (flag) {
-    cudaMemset(op->opflag.p, 0, sizeof(int));
-    set_error("an operator apply gave up waiting for its asynchronous projector copies (results invalid)");
-    return SGW_ERR_CUDA;
-  }
-  return s;
-}
 
 // Sum the per-kernel event pairs of the finished solve (stream already synchronised).
 void collect_kernel_times(sgw_operator* op) {
@@ -239,7 +225,6 @@ static sgw_status upload_pw(sgw_operator* op, const sgw_pw_operator_desc* d, con
   v.pan = npan > 0 ? pan.as<cplx<T>>() : nullptr;
   v.pan_pitch = pan_pitch;
   v.pan_rows = pan_rows;
-  v.err = op->opflag.as<int>();
   v.npw = npw;
   v.npwx = npwx;
   v.nr1 = d->nr1;
@@ -355,11 +340,6 @@ static sgw_status create_pw(const sgw_pw_operator_desc* d, sgw_operator** out) {
     std::vector<unsigned long long> zm(ncol, 0ull);
     for (int g = 0; g < d->npw; ++g) zm[gcol[g]] |= 1ull << gi3[g];
     s = op->zmask.upload(zm.data(), zm.size());
-  }
-  if (s == SGW_OK && (s = op->opflag.ensure(sizeof(int))) == SGW_OK &&
-      cudaMemset(op->opflag.p, 0, sizeof(int)) != cudaSuccess) {
-    set_error("cudaMemset of the operator's error flag failed");
-    s = SGW_ERR_CUDA;
   }
   if (s == SGW_OK)
     s = upload_pw<double>(op, d, gcol, gi3, colpos, i1v, ncol, ldz, pitch, p1, p2, p3, op->g2k64, op->vrs64,
@@ -820,7 +800,7 @@ sgw_status sgw_operator_destroy(sgw_operator* op) {
   if (op->copy_stream) cudaStreamSynchronize(op->copy_stream);
   DevBuf* bufs[] = {&op->ymask, &op->zmask, &op->gcol, &op->gi3, &op->colpos, &op->i1list, &op->g2k64, &op->g2k32, &op->vrs64, &op->vrs32,
                     &op->vkb64, &op->vkb32, &op->dvan64, &op->dvan32, &op->evq64, &op->evq32, &op->tw64, &op->tw32,
-                    &op->a64, &op->a32, &op->pan64, &op->pan32, &op->opflag, &op->ws64.vec, &op->ws64.coef, &op->ws64.col, &op->ws64.counter,
+                    &op->a64, &op->a32, &op->pan64, &op->pan32, &op->ws64.vec, &op->ws64.coef, &op->ws64.col, &op->ws64.counter,
                     &op->ws32.vec, &op->ws32.coef, &op->ws32.col, &op->ws32.counter, &op->st_bb, &op->st_sigma,
                     &op->st_xx, &op->st_ierr, &op->st_iters, &op->st_misc, &op->st_misc2, &op->st_misc3,
                     &op->st_ref, &op->st_ref2, &op->st_resid, &op->nlkq, &op->lt_psi, &op->lt_box, &op->lt_nlk, &op->lt_evc, &op->lt_dv, &op->lt_bb,
@@ -872,7 +852,7 @@ sgw_status sgw_operator_apply(sgw_operator* op, sgw_zcomplex sigma, int32_t m, c
   try {
     CallScope cs(op);
     if (cs.status() != SGW_OK) return cs.status();
-    return finish_call(op, apply_host(op, sigma, m, x, ldx_in, ax, ldx_out));
+    return apply_host(op, sigma, m, x, ldx_in, ax, ldx_out);
   } catch (...) {
     set_error("host exception in sgw_operator_apply");
     return SGW_ERR_NOMEM;
@@ -884,7 +864,7 @@ sgw_status sgw_operator_apply_ex(sgw_operator* op, int32_t precision, int32_t me
   try {
     CallScope cs(op);
     if (cs.status() != SGW_OK) return cs.status();
-    return finish_call(op, apply_ex(op, precision, memory, sigma, m, x, ldx_in, ax, ldx_out));
+    return apply_ex(op, precision, memory, sigma, m, x, ldx_in, ax, ldx_out);
   } catch (...) {
     set_error("host exception in sgw_operator_apply_ex");
     return SGW_ERR_NOMEM;
@@ -897,8 +877,7 @@ sgw_status sgw_bicgstab(sgw_operator* op, int32_t lmax, double threshold, int32_
   try {
     CallScope cs(op);
     if (cs.status() != SGW_OK) return cs.status();
-    sgw_status s =
-        finish_call(op, single_bicgstab(op, lmax, threshold, max_iter, bb, n, sigma, num_shift, xx, ldx, ierr));
+    sgw_status s = single_bicgstab(op, lmax, threshold, max_iter, bb, n, sigma, num_shift, xx, ldx, ierr);
     return s == SGW_OK ? (sgw_status)*ierr : s;
   } catch (...) {
     set_error("host exception in sgw_bicgstab");
@@ -912,7 +891,7 @@ sgw_status sgw_linear_solver(sgw_operator* op, double threshold, int32_t max_ite
   try {
     CallScope cs(op);
     if (cs.status() != SGW_OK) return cs.status();
-    sgw_status s = finish_call(op, single_sgw(op, threshold, max_iter, bb, n, sigma, num_shift, xx, ldx, ierr));
+    sgw_status s = single_sgw(op, threshold, max_iter, bb, n, sigma, num_shift, xx, ldx, ierr);
     return s == SGW_OK ? (sgw_status)*ierr : s;
   } catch (...) {
     set_error("host exception in sgw_linear_solver");
@@ -957,7 +936,7 @@ sgw_status sgw_solve_batch(sgw_operator* op, const sgw_batch_desc* desc) {
   try {
     CallScope cs(op);
     if (cs.status() != SGW_OK) return cs.status();
-    return finish_call(op, solve_batch(op, desc));
+    return solve_batch(op, desc);
   } catch (...) {
     set_error("host exception in sgw_solve_batch");
     return SGW_ERR_NOMEM;
@@ -968,7 +947,7 @@ sgw_status sgw_solve_batch_ex(sgw_operator* op, const sgw_batch_desc* desc, cons
   try {
     CallScope cs(op);
     if (cs.status() != SGW_OK) return cs.status();
-    return finish_call(op, solve_batch(op, desc, opt));
+    return solve_batch(op, desc, opt);
   } catch (...) {
     set_error("host exception in sgw_solve_batch_ex");
     return SGW_ERR_NOMEM;

@@ -131,7 +131,7 @@ struct sgw_operator {
   // tables
   unsigned long long xmask = 0;
   sgw::DevBuf nlkq, ymask, zmask, gcol, gi3, colpos, i1list, g2k64, g2k32, vrs64, vrs32, vkb64, vkb32, dvan64, dvan32, evq64, evq32,
-      tw64, tw32, a64, a32, pan64, pan32, opflag;
+      tw64, tw32, a64, a32, pan64, pan32;
   sgw::PwView<double> pw64{};
   sgw::PwView<float> pw32{};
   sgw::DenseView<double> dn64{};
@@ -203,9 +203,6 @@ class CallScope {
 // Sum the per-kernel event pairs of the last call into kernel_ms / kernel_launches
 // (the handle's stream must be synchronised).
 void collect_kernel_times(sgw_operator* op);
-// The status of a call that ran operator applies, turned into SGW_ERR_CUDA when
-// an apply gave up one of its bounded waits (the flag is cleared).
-sgw_status finish_call(sgw_operator* op, sgw_status s);
 // `stream` waits for the work queued so far on `caller` (event `ev` is reused).
 sgw_status order_after(cudaStream_t stream, cudaStream_t caller, cudaEvent_t ev);
 

@@ -554,7 +554,7 @@ sgw_status sgw_solve_adjoint(sgw_operator* op, const sgw_adjoint_desc* desc) {
   try {
     sgw::CallScope cs(op);
     if (cs.status() != SGW_OK) return cs.status();
-    return sgw::finish_call(op, sgw::solve_adjoint(op, desc));
+    return sgw::solve_adjoint(op, desc);
   } catch (...) {
     sgw::set_error("host exception in sgw_solve_adjoint");
     return SGW_ERR_NOMEM;
@@ -576,7 +576,7 @@ sgw_status sgw_green_function(sgw_operator* op, const sgw_green_desc* desc) {
   try {
     sgw::CallScope cs(op);
     if (cs.status() != SGW_OK) return cs.status();
-    return sgw::finish_call(op, sgw::green_function(op, desc));
+    return sgw::green_function(op, desc);
   } catch (...) {
     sgw::set_error("host exception in sgw_green_function");
     return SGW_ERR_NOMEM;

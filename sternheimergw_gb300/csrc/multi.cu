@@ -845,13 +845,7 @@ sgw_status sgw_multi_create(int32_t nsys, sgw_operator* const* ops, const sgw_ba
 
 sgw_status sgw_multi_run(sgw_multi* plan, double* total_ms, double* sys_ms) {
   try {
-    const sgw_status s = sgw::multi_run(plan, total_ms, sys_ms);
-    if (s < 0 || !plan) return s;
-    for (sgw_operator* op : plan->ops) {
-      const sgw_status f = sgw::finish_call(op, s);
-      if (f != s) return f;
-    }
-    return s;
+    return sgw::multi_run(plan, total_ms, sys_ms);
   } catch (...) {
     sgw::set_error("host exception in sgw_multi_run");
     return SGW_ERR_NOMEM;
@@ -900,8 +894,8 @@ sgw_status sgw_operator_autotune(sgw_operator* op, int32_t precision, sgw_tune_r
     }
     sgw::CallScope cs(op);
     if (cs.status() != SGW_OK) return cs.status();
-    if (precision == 0) return sgw::finish_call(op, sgw::tune<double>(op, result));
-    if (precision == 1) return sgw::finish_call(op, sgw::tune<float>(op, result));
+    if (precision == 0) return sgw::tune<double>(op, result);
+    if (precision == 1) return sgw::tune<float>(op, result);
     sgw::set_error("precision must be 0 (FP64 kernels) or 1 (FP32 kernels)");
     return SGW_ERR_ARG;
   } catch (...) {

@@ -108,5 +108,5 @@ extern "C" sgw_status sgw_solve_batch_noalloc(sgw_operator* op, const sgw_batch_
   SGW_CK(cudaEventElapsedTime(&ms, op->ev0, op->ev1));
   op->last_ms = ms;
   collect_kernel_times(op);
-  return finish_call(op, SGW_OK);
+  return SGW_OK;
 }

@@ -48,7 +48,6 @@ struct PwView {
   // pan_pitch odd (>= nkb + nocc), pan_rows >= npwx (zero rows after npw).
   const cplx<T>* pan;
   int pan_pitch, pan_rows;
-  int* err;            // set to 1 when a bounded wait on an asynchronous copy gives up
   double alpha_pv;
   FftPlan p1, p2, p3;
   const cplx<T>* tw;   // [nr1 | nr2 | nr3] exp(+2 pi i e / n)
@@ -68,48 +67,18 @@ __host__ __device__ inline int pw_smem_small(const PwView<T>& op, int ng) {
 }
 
 // ---------------------------------------------------------------------------
-// Bulk asynchronous copies global -> shared memory, completed on an mbarrier
-// (cp.async.bulk + mbarrier complete_tx, issued by one thread).
+// Asynchronous 16-byte copies global -> shared memory (cp.async, commit /
+// wait groups): every thread copies its share of a chunk, so completion is
+// per thread and a CTA barrier makes the whole chunk visible.
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
-
-__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
 }
-__device__ __forceinline__ void mbar_fence_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
-// orders earlier generic-proxy shared-memory accesses before later async-proxy ones
-__device__ __forceinline__ void fence_proxy_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
-__device__ __forceinline__ void mbar_expect_tx(unsigned long long* bar, unsigned bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
-}
-// dst, src 16-byte aligned; bytes a multiple of 16
-__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned bytes, unsigned long long* bar) {
-  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                   smem_u32(dst)),
-               "l"(src), "r"(bytes), "r"(smem_u32(bar))
-               : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, unsigned parity) {
-  unsigned ok;
-  asm volatile(
-      "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
-      : "=r"(ok)
-      : "r"(smem_u32(bar)), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-// Wait for phase `parity` of an mbarrier, at most ~2^32 SM cycles (about two
-// seconds); on a timeout *err is set and the caller goes on with whatever the
-// buffer holds (the host then reports the call as failed).
-__device__ __forceinline__ void mbar_wait(unsigned long long* bar, unsigned parity, int* err) {
-  if (mbar_try_wait(bar, parity)) return;
-  const long long t0 = clock64();
-  while (!mbar_try_wait(bar, parity)) {
-    if (clock64() - t0 > (1LL << 32)) {
-      if (err) atomicExch(err, 1);
-      return;
-    }
-  }
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
 }
 
 // CTA-wide sum of a double2 partial; result broadcast to every thread.
@@ -221,14 +190,14 @@ __device__ void pw_apply_cta(const PwView<T>& op, const int NG, const cplx<T>* _
 
 // Staging plan of the projector panel in a shared-memory region (the plane
 // buffers, idle before and after the FFT): optionally the input vector (npw
-// elements), then `nst` stages of G panel rows each, filled by bulk
+// elements), then `nst` (2 or 3) stages of G panel rows each, filled by
 // asynchronous copies while the CTA works on the previous stage.  ok = false
 // when the region is too small for two stages or the projectors outnumber
 // the threads; the apply then streams the projectors from L2 directly.
 template <typename T>
 struct PanelPlan {
   int npan, G, nst, nchunk;
-  unsigned chunk_bytes;
+  int chunk_granules;  // 16-byte units per chunk
   cplx<T>* xs;
   cplx<T>* stage;
   bool ok;
@@ -251,11 +220,12 @@ __device__ __forceinline__ PanelPlan<T> panel_plan(const PwView<T>& op, int npan
     if ((int)blockDim.x % G) continue;
     const long long ce = (long long)G * op.pan_pitch;
     const long long nst = ce > 0 ? (elems - xe) / ce : 0;
-    if (nst >= 2) {
+    // the projection's partial sums (at most blockDim values) reuse the stages
+    if (nst >= 2 && nst * ce >= (long long)blockDim.x) {
       pl.G = G;
-      pl.nst = (int)(nst < 4 ? nst : 4);
+      pl.nst = nst >= 3 ? 3 : 2;
       pl.nchunk = (op.npw + G - 1) / G;
-      pl.chunk_bytes = (unsigned)(ce * (long long)sizeof(cplx<T>));
+      pl.chunk_granules = (int)(ce * (long long)sizeof(cplx<T>) / 16);
       pl.xs = base;
       pl.stage = base + xe;
       pl.ok = true;
@@ -265,15 +235,32 @@ __device__ __forceinline__ PanelPlan<T> panel_plan(const PwView<T>& op, int npan
   return pl;
 }
 
-// Issue the bulk copy of panel chunk c into its stage (one thread).
+// Every thread copies its 16-byte granules of panel chunk c (if c < nchunk)
+// into the chunk's stage, then commits a group (empty past the last chunk, so
+// the count of pending groups stays the same in every iteration).
 template <typename T>
-__device__ __forceinline__ void panel_issue(const PwView<T>& op, const PanelPlan<T>& pl, int c,
-                                            unsigned long long* bars) {
-  const int k = c % pl.nst;
-  cplx<T>* dst = pl.stage + (size_t)k * pl.G * op.pan_pitch;
-  fence_proxy_async_smem();
-  mbar_expect_tx(&bars[k], pl.chunk_bytes);
-  bulk_g2s(dst, op.pan + (size_t)c * pl.G * op.pan_pitch, pl.chunk_bytes, &bars[k]);
+__device__ __forceinline__ void panel_load(const PwView<T>& op, const PanelPlan<T>& pl, int c) {
+  if (c < pl.nchunk) {
+    const int k = c % pl.nst;
+    char* dst = reinterpret_cast<char*>(pl.stage + (size_t)k * pl.G * op.pan_pitch);
+    const char* src = reinterpret_cast<const char*>(op.pan + (size_t)c * pl.G * op.pan_pitch);
+    for (int q = threadIdx.x; q < pl.chunk_granules; q += blockDim.x) cp_async16(dst + 16 * (size_t)q, src + 16 * (size_t)q);
+  }
+  cp_async_commit();
+}
+
+// Runs body(c, stage) over the panel's chunks with nst - 1 chunks in flight.
+template <int NS, typename T, class Body>
+__device__ __forceinline__ void panel_pipeline(const PwView<T>& op, const PanelPlan<T>& pl, Body&& body) {
+  for (int c = 0; c < NS - 1; ++c) panel_load(op, pl, c);
+  for (int c = 0; c < pl.nchunk; ++c) {
+    panel_load(op, pl, c + NS - 1);
+    cp_async_wait<NS - 1>();  // this thread's copies of chunk c have landed
+    __syncthreads();          // ... and every other thread's
+    body(c, pl.stage + (size_t)(c % NS) * pl.G * op.pan_pitch);
+    __syncthreads();          // the stage is read before chunk c + NS overwrites it
+  }
+  cp_async_wait<0>();
 }
 
 // bec[i] = D_i <beta_i|in> (i < nkb), alpha_pv <evq|in> (nkb <= i < npan) from the
@@ -282,39 +269,30 @@ __device__ __forceinline__ void panel_issue(const PwView<T>& op, const PanelPlan
 // vector is left staged in pl.xs.
 template <typename T>
 __device__ void panel_project(const PwView<T>& op, const PanelPlan<T>& pl, const cplx<T>* __restrict__ in,
-                              cplx<T>* bec, unsigned long long* bars) {
+                              cplx<T>* bec) {
   const int tid = threadIdx.x, nt = blockDim.x;
   const int npan = pl.npan, pitch = op.pan_pitch, G = pl.G;
-  if (tid == 0) {
-    for (int k = 0; k < pl.nst; ++k) mbar_init(&bars[k], 1);
-    mbar_fence_init();
-  }
   for (int g = tid; g < op.npw; g += nt) pl.xs[g] = in[g];
-  __syncthreads();
-  if (tid == 0)
-    for (int c = 0; c < pl.nst && c < pl.nchunk; ++c) panel_issue(op, pl, c, bars);
   const int nsub = nt / npan;
   const int i = tid % npan, sg = tid / npan;
   const bool act = tid < npan * nsub;
   cplx<T> acc0 = {0, 0}, acc1 = {0, 0};
-  for (int c = 0; c < pl.nchunk; ++c) {
-    const int k = c % pl.nst;
-    mbar_wait(&bars[k], (unsigned)((c / pl.nst) & 1), op.err);
-    const cplx<T>* P = pl.stage + (size_t)k * G * pitch;
+  auto body = [&](int c, const cplx<T>* P) {
+    if (!act) return;
     const int g0 = c * G;
     const int rows = min(G, op.npw - g0);
-    if (act) {
-      int r = sg;
-      for (; r + nsub < rows; r += 2 * nsub) {  // two chains in flight
-        cfma_conj(acc0, P[(size_t)r * pitch + i], pl.xs[g0 + r]);
-        cfma_conj(acc1, P[(size_t)(r + nsub) * pitch + i], pl.xs[g0 + r + nsub]);
-      }
-      if (r < rows) cfma_conj(acc0, P[(size_t)r * pitch + i], pl.xs[g0 + r]);
+    int r = sg;
+    for (; r + nsub < rows; r += 2 * nsub) {  // two chains in flight
+      cfma_conj(acc0, P[(size_t)r * pitch + i], pl.xs[g0 + r]);
+      cfma_conj(acc1, P[(size_t)(r + nsub) * pitch + i], pl.xs[g0 + r + nsub]);
     }
-    __syncthreads();
-    if (tid == 0 && c + pl.nst < pl.nchunk) panel_issue(op, pl, c + pl.nst, bars);
-  }
-  // every copy has completed and been read: the stages hold the partial sums now
+    if (r < rows) cfma_conj(acc0, P[(size_t)r * pitch + i], pl.xs[g0 + r]);
+  };
+  if (pl.nst >= 3)
+    panel_pipeline<3>(op, pl, body);
+  else
+    panel_pipeline<2>(op, pl, body);
+  // every copy has landed and been read: the stages hold the partial sums now
   cplx<T>* part = pl.stage;
   if (act) part[sg * npan + i] = acc0 + acc1;
   __syncthreads();
@@ -332,22 +310,14 @@ __device__ void panel_project(const PwView<T>& op, const PanelPlan<T>& pl, const
 template <typename T>
 __device__ void panel_gather(const PwView<T>& op, const PanelPlan<T>& pl, const cplx<T>* __restrict__ in,
                              cplx<T>* __restrict__ out, cplx<T>* __restrict__ out2, zcd sigma, const cplx<T>* bec,
-                             const cplx<T>* col, unsigned long long* bars) {
+                             const cplx<T>* col) {
   const int tid = threadIdx.x, nt = blockDim.x;
   const int npan = pl.npan, pitch = op.pan_pitch, G = pl.G, Q = nt / G;
-  if (tid == 0) {
-    for (int k = 0; k < pl.nst; ++k) mbar_init(&bars[k], 1);
-    mbar_fence_init();
-    for (int c = 0; c < pl.nst && c < pl.nchunk; ++c) panel_issue(op, pl, c, bars);
-  }
-  __syncthreads();  // no thread waits on a barrier before it is initialised
   const T scale = (T)(1.0 / (double)op.nnr);
   const cplx<T> sgm = ccast<T>(sigma);
   const int r = tid / Q, q = tid % Q;
-  for (int c = 0; c < pl.nchunk; ++c) {
-    const int k = c % pl.nst;
-    mbar_wait(&bars[k], (unsigned)((c / pl.nst) & 1), op.err);
-    const cplx<T>* P = pl.stage + (size_t)k * G * pitch + (size_t)r * pitch;
+  auto body = [&](int c, const cplx<T>* S) {
+    const cplx<T>* P = S + (size_t)r * pitch;
     cplx<T> sum = {0, 0};
     for (int j = q; j < npan; j += Q) cfma(sum, P[j], bec[j]);
     for (int o = Q >> 1; o > 0; o >>= 1) {
@@ -361,9 +331,11 @@ __device__ void panel_gather(const PwView<T>& op, const PanelPlan<T>& pl, const 
       out[g] = res;
       if (out2) out2[g] = res;
     }
-    __syncthreads();
-    if (tid == 0 && c + pl.nst < pl.nchunk) panel_issue(op, pl, c + pl.nst, bars);
-  }
+  };
+  if (pl.nst >= 3)
+    panel_pipeline<3>(op, pl, body);
+  else
+    panel_pipeline<2>(op, pl, body);
 }
 
 // Line-per-thread variant of pw_apply_cta for box lengths with a register
@@ -388,15 +360,14 @@ __device__ void pw_apply_cta_lines(const PwView<T>& op, const int PF, const cplx
   const int ldz = op.ldz, pitch = op.pitch, psz = op.nr2 * op.pitch;
 
   // The projectors: with a staging plan they stream through the idle plane
-  // buffers by bulk asynchronous copies (panel_project / panel_gather);
+  // buffers by asynchronous copies (panel_project / panel_gather);
   // otherwise each warp takes one projection and streams its row from L2.
-  __shared__ __align__(8) unsigned long long s_bars[4];
   const int npan = op.nkb + nocc;
   const long long plane_elems = (long long)PF * psz;
   const PanelPlan<T> plp = panel_plan<T>(op, npan, planes, plane_elems, true);
   const cplx<T>* src = in;
   if (plp.ok) {
-    panel_project<T>(op, plp, in, bec, s_bars);
+    panel_project<T>(op, plp, in, bec);
     src = plp.xs;
   } else {
     // <beta_i|psi> D_i and alpha_pv <evq_v|psi>, one warp per projection; the
@@ -522,7 +493,7 @@ __device__ void pw_apply_cta_lines(const PwView<T>& op, const int PF, const cplx
 
   const PanelPlan<T> plg = panel_plan<T>(op, npan, planes, plane_elems, false);
   if (plg.ok) {
-    panel_gather<T>(op, plg, in, out, out2, sigma, bec, col, s_bars);
+    panel_gather<T>(op, plg, in, out, out2, sigma, bec, col);
     return;
   }
   const T scale = (T)(1.0 / (double)op.nnr);
