@@ -158,7 +158,6 @@ CallScope::~CallScope() {
   if (dev_ >= 0 && prev_ >= 0) cudaSetDevice(prev_);
 }
 
-
 // Sum the per-kernel event pairs of the finished solve (stream already synchronised).
 void collect_kernel_times(sgw_operator* op) {
   for (int k : {K_MSBICG_F64, K_MSBICG_F32, K_RESIDUAL_F64, K_COPY_IN, K_COPY_OUT}) {  // rhs/chi/vjp keep their own
@@ -180,7 +179,7 @@ static sgw_status upload_pw(sgw_operator* op, const sgw_pw_operator_desc* d, con
                             const std::vector<int>& gi3_h, const std::vector<int>& colpos_h,
                             const std::vector<int>& i1_h, int ncol, int ldz, int pitch, const FftPlan& p1,
                             const FftPlan& p2, const FftPlan& p3, DevBuf& g2k, DevBuf& vrs, DevBuf& vkb, DevBuf& dvan,
-                            DevBuf& evq, DevBuf& tw, DevBuf& pan) {
+                            DevBuf& evq, DevBuf& tw) {
   const int npw = d->npw, npwx = op->npwx;
   const size_t nnr = (size_t)d->nr1 * d->nr2 * d->nr3;
   std::vector<T> g2(npw), vr(nnr), dv(std::max(d->nkb, 1));
@@ -199,16 +198,6 @@ static sgw_status upload_pw(sgw_operator* op, const sgw_pw_operator_desc* d, con
       const sgw_zcomplex z = d->evq[(size_t)v * d->npwx + g];
       ev[(size_t)v * npwx + g] = cplx<T>{(T)z.re, (T)z.im};
     }
-  // the same projectors g-major for the staged line apply: rows padded to a
-  // multiple of 128 (whole chunks), an odd row pitch (shared-memory banks)
-  const int npan = d->nkb + d->nbnd_occ;
-  const int pan_pitch = npan > 0 ? (npan | 1) : 0;
-  const int pan_rows = (npwx + 127) / 128 * 128;
-  std::vector<cplx<T>> pv((size_t)std::max(pan_pitch, 1) * pan_rows, cplx<T>{0, 0});
-  for (int g = 0; g < npw; ++g) {
-    for (int i = 0; i < d->nkb; ++i) pv[(size_t)g * pan_pitch + i] = kb[(size_t)i * npwx + g];
-    for (int v = 0; v < d->nbnd_occ; ++v) pv[(size_t)g * pan_pitch + d->nkb + v] = ev[(size_t)v * npwx + g];
-  }
   std::vector<cplx<T>> twv;
   twiddles<T>(d->nr1, twv);
   twiddles<T>(d->nr2, twv);
@@ -220,11 +209,7 @@ static sgw_status upload_pw(sgw_operator* op, const sgw_pw_operator_desc* d, con
   if ((s = dvan.upload(dv.data(), dv.size())) != SGW_OK) return s;
   if ((s = evq.upload(ev.data(), ev.size())) != SGW_OK) return s;
   if ((s = tw.upload(twv.data(), twv.size())) != SGW_OK) return s;
-  if (npan > 0 && (s = pan.upload(pv.data(), pv.size())) != SGW_OK) return s;
   PwView<T>& v = pwview<T>(op);
-  v.pan = npan > 0 ? pan.as<cplx<T>>() : nullptr;
-  v.pan_pitch = pan_pitch;
-  v.pan_rows = pan_rows;
   v.npw = npw;
   v.npwx = npwx;
   v.nr1 = d->nr1;
@@ -343,10 +328,10 @@ static sgw_status create_pw(const sgw_pw_operator_desc* d, sgw_operator** out) {
   }
   if (s == SGW_OK)
     s = upload_pw<double>(op, d, gcol, gi3, colpos, i1v, ncol, ldz, pitch, p1, p2, p3, op->g2k64, op->vrs64,
-                          op->vkb64, op->dvan64, op->evq64, op->tw64, op->pan64);
+                          op->vkb64, op->dvan64, op->evq64, op->tw64);
   if (s == SGW_OK)
     s = upload_pw<float>(op, d, gcol, gi3, colpos, i1v, ncol, ldz, pitch, p1, p2, p3, op->g2k32, op->vrs32,
-                         op->vkb32, op->dvan32, op->evq32, op->tw32, op->pan32);
+                         op->vkb32, op->dvan32, op->evq32, op->tw32);
   if (s == SGW_OK && (op->shape64.ng == 0 || op->shape32.ng == 0)) {
     set_error("FFT plane does not fit in shared memory");
     s = SGW_ERR_UNSUPPORTED;
@@ -800,7 +785,7 @@ sgw_status sgw_operator_destroy(sgw_operator* op) {
   if (op->copy_stream) cudaStreamSynchronize(op->copy_stream);
   DevBuf* bufs[] = {&op->ymask, &op->zmask, &op->gcol, &op->gi3, &op->colpos, &op->i1list, &op->g2k64, &op->g2k32, &op->vrs64, &op->vrs32,
                     &op->vkb64, &op->vkb32, &op->dvan64, &op->dvan32, &op->evq64, &op->evq32, &op->tw64, &op->tw32,
-                    &op->a64, &op->a32, &op->pan64, &op->pan32, &op->ws64.vec, &op->ws64.coef, &op->ws64.col, &op->ws64.counter,
+                    &op->a64, &op->a32, &op->ws64.vec, &op->ws64.coef, &op->ws64.col, &op->ws64.counter,
                     &op->ws32.vec, &op->ws32.coef, &op->ws32.col, &op->ws32.counter, &op->st_bb, &op->st_sigma,
                     &op->st_xx, &op->st_ierr, &op->st_iters, &op->st_misc, &op->st_misc2, &op->st_misc3,
                     &op->st_ref, &op->st_ref2, &op->st_resid, &op->nlkq, &op->lt_psi, &op->lt_box, &op->lt_nlk, &op->lt_evc, &op->lt_dv, &op->lt_bb,

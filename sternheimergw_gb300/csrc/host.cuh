@@ -131,7 +131,7 @@ struct sgw_operator {
   // tables
   unsigned long long xmask = 0;
   sgw::DevBuf nlkq, ymask, zmask, gcol, gi3, colpos, i1list, g2k64, g2k32, vrs64, vrs32, vkb64, vkb32, dvan64, dvan32, evq64, evq32,
-      tw64, tw32, a64, a32, pan64, pan32;
+      tw64, tw32, a64, a32;
   sgw::PwView<double> pw64{};
   sgw::PwView<float> pw32{};
   sgw::DenseView<double> dn64{};

@@ -43,11 +43,6 @@ struct PwView {
   const T* dvan;       // [nkb]
   int nocc;
   const cplx<T>* evq;  // [nocc][npwx]
-  // The same projectors as one g-major panel for the staged line apply:
-  // pan[g][j] = vkb_j(g) (j < nkb), evq_(j-nkb)(g) (j < nkb + nocc), 0 beyond;
-  // pan_pitch odd (>= nkb + nocc), pan_rows >= npwx (zero rows after npw).
-  const cplx<T>* pan;
-  int pan_pitch, pan_rows;
   double alpha_pv;
   FftPlan p1, p2, p3;
   const cplx<T>* tw;   // [nr1 | nr2 | nr3] exp(+2 pi i e / n)
@@ -64,21 +59,6 @@ __host__ __device__ inline int pw_cpos_units(const PwView<T>& op) {
 template <typename T>
 __host__ __device__ inline int pw_smem_small(const PwView<T>& op, int ng) {
   return op.nr1 + op.nr2 + op.nr3 + op.nkb + op.nocc + pw_cpos_units(op) + ng * op.nr2 * op.pitch;
-}
-
-// ---------------------------------------------------------------------------
-// Asynchronous 16-byte copies global -> shared memory (cp.async, commit /
-// wait groups): every thread copies its share of a chunk, so completion is
-// per thread and a CTA barrier makes the whole chunk visible.
-// ---------------------------------------------------------------------------
-__device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
-__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void cp_async_wait() {
-  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
 }
 
 // CTA-wide sum of a double2 partial; result broadcast to every thread.
@@ -188,156 +168,6 @@ __device__ void pw_apply_cta(const PwView<T>& op, const int NG, const cplx<T>* _
   __syncthreads();
 }
 
-// Staging plan of the projector panel in a shared-memory region (the plane
-// buffers, idle before and after the FFT): optionally the input vector (npw
-// elements), then `nst` (2 or 3) stages of G panel rows each, filled by
-// asynchronous copies while the CTA works on the previous stage.  ok = false
-// when the region is too small for two stages or the projectors outnumber
-// the threads; the apply then streams the projectors from L2 directly.
-template <typename T>
-struct PanelPlan {
-  int npan, G, nst, nchunk;
-  int chunk_granules;  // 16-byte units per chunk
-  cplx<T>* xs;
-  cplx<T>* stage;
-  bool ok;
-};
-
-template <typename T>
-__device__ __forceinline__ PanelPlan<T> panel_plan(const PwView<T>& op, int npan, cplx<T>* region, long long elems,
-                                                   bool stage_input) {
-  PanelPlan<T> pl{};
-  pl.npan = npan;
-  pl.ok = false;
-  if (!op.pan || npan < 1 || npan > (int)blockDim.x) return pl;
-  // 128-byte aligned start (the region may start at an 8-byte boundary in FP32)
-  const size_t a = reinterpret_cast<size_t>(region);
-  const long long skip = (long long)(((a + 127) & ~(size_t)127) - a) / (long long)sizeof(cplx<T>);
-  cplx<T>* base = region + skip;
-  elems -= skip;
-  const long long xe = stage_input ? ((long long)op.npw + 15) / 16 * 16 : 0;
-  for (int G : {64, 32, 16}) {
-    if ((int)blockDim.x % G) continue;
-    const long long ce = (long long)G * op.pan_pitch;
-    const long long nst = ce > 0 ? (elems - xe) / ce : 0;
-    // the projection's partial sums (at most blockDim values) reuse the stages
-    if (nst >= 2 && nst * ce >= (long long)blockDim.x) {
-      pl.G = G;
-      pl.nst = nst >= 3 ? 3 : 2;
-      pl.nchunk = (op.npw + G - 1) / G;
-      pl.chunk_granules = (int)(ce * (long long)sizeof(cplx<T>) / 16);
-      pl.xs = base;
-      pl.stage = base + xe;
-      pl.ok = true;
-      return pl;
-    }
-  }
-  return pl;
-}
-
-// Every thread copies its 16-byte granules of panel chunk c (if c < nchunk)
-// into the chunk's stage, then commits a group (empty past the last chunk, so
-// the count of pending groups stays the same in every iteration).
-template <typename T>
-__device__ __forceinline__ void panel_load(const PwView<T>& op, const PanelPlan<T>& pl, int c) {
-  if (c < pl.nchunk) {
-    const int k = c % pl.nst;
-    char* dst = reinterpret_cast<char*>(pl.stage + (size_t)k * pl.G * op.pan_pitch);
-    const char* src = reinterpret_cast<const char*>(op.pan + (size_t)c * pl.G * op.pan_pitch);
-    for (int q = threadIdx.x; q < pl.chunk_granules; q += blockDim.x) cp_async16(dst + 16 * (size_t)q, src + 16 * (size_t)q);
-  }
-  cp_async_commit();
-}
-
-// Runs body(c, stage) over the panel's chunks with nst - 1 chunks in flight.
-template <int NS, typename T, class Body>
-__device__ __forceinline__ void panel_pipeline(const PwView<T>& op, const PanelPlan<T>& pl, Body&& body) {
-  for (int c = 0; c < NS - 1; ++c) panel_load(op, pl, c);
-  for (int c = 0; c < pl.nchunk; ++c) {
-    panel_load(op, pl, c + NS - 1);
-    cp_async_wait<NS - 1>();  // this thread's copies of chunk c have landed
-    __syncthreads();          // ... and every other thread's
-    body(c, pl.stage + (size_t)(c % NS) * pl.G * op.pan_pitch);
-    __syncthreads();          // the stage is read before chunk c + NS overwrites it
-  }
-  cp_async_wait<0>();
-}
-
-// bec[i] = D_i <beta_i|in> (i < nkb), alpha_pv <evq|in> (nkb <= i < npan) from the
-// staged panel.  Thread (i, s) accumulates the rows r = s (mod nsub) of every
-// chunk; the nsub partials of each i are summed in a fixed order.  The input
-// vector is left staged in pl.xs.
-template <typename T>
-__device__ void panel_project(const PwView<T>& op, const PanelPlan<T>& pl, const cplx<T>* __restrict__ in,
-                              cplx<T>* bec) {
-  const int tid = threadIdx.x, nt = blockDim.x;
-  const int npan = pl.npan, pitch = op.pan_pitch, G = pl.G;
-  for (int g = tid; g < op.npw; g += nt) pl.xs[g] = in[g];
-  const int nsub = nt / npan;
-  const int i = tid % npan, sg = tid / npan;
-  const bool act = tid < npan * nsub;
-  cplx<T> acc0 = {0, 0}, acc1 = {0, 0};
-  auto body = [&](int c, const cplx<T>* P) {
-    if (!act) return;
-    const int g0 = c * G;
-    const int rows = min(G, op.npw - g0);
-    int r = sg;
-    for (; r + nsub < rows; r += 2 * nsub) {  // two chains in flight
-      cfma_conj(acc0, P[(size_t)r * pitch + i], pl.xs[g0 + r]);
-      cfma_conj(acc1, P[(size_t)(r + nsub) * pitch + i], pl.xs[g0 + r + nsub]);
-    }
-    if (r < rows) cfma_conj(acc0, P[(size_t)r * pitch + i], pl.xs[g0 + r]);
-  };
-  if (pl.nst >= 3)
-    panel_pipeline<3>(op, pl, body);
-  else
-    panel_pipeline<2>(op, pl, body);
-  // every copy has landed and been read: the stages hold the partial sums now
-  cplx<T>* part = pl.stage;
-  if (act) part[sg * npan + i] = acc0 + acc1;
-  __syncthreads();
-  for (int j = tid; j < npan; j += nt) {
-    cplx<T> sum = {0, 0};
-    for (int q = 0; q < nsub; ++q) sum += part[q * npan + j];
-    bec[j] = (j < op.nkb ? op.dvan[j] : (T)op.alpha_pv) * sum;
-  }
-  __syncthreads();
-}
-
-// out[g] = (|k+G|^2 + sigma) in[g] + scale col[...] + sum_i pan[g][i] bec[i] from the
-// staged panel: Q = blockDim / G threads per row, each over the columns i = q (mod Q),
-// combined with shuffles.
-template <typename T>
-__device__ void panel_gather(const PwView<T>& op, const PanelPlan<T>& pl, const cplx<T>* __restrict__ in,
-                             cplx<T>* __restrict__ out, cplx<T>* __restrict__ out2, zcd sigma, const cplx<T>* bec,
-                             const cplx<T>* col) {
-  const int tid = threadIdx.x, nt = blockDim.x;
-  const int npan = pl.npan, pitch = op.pan_pitch, G = pl.G, Q = nt / G;
-  const T scale = (T)(1.0 / (double)op.nnr);
-  const cplx<T> sgm = ccast<T>(sigma);
-  const int r = tid / Q, q = tid % Q;
-  auto body = [&](int c, const cplx<T>* S) {
-    const cplx<T>* P = S + (size_t)r * pitch;
-    cplx<T> sum = {0, 0};
-    for (int j = q; j < npan; j += Q) cfma(sum, P[j], bec[j]);
-    for (int o = Q >> 1; o > 0; o >>= 1) {
-      sum.re += __shfl_xor_sync(0xffffffffu, sum.re, o);
-      sum.im += __shfl_xor_sync(0xffffffffu, sum.im, o);
-    }
-    const int g = c * G + r;
-    if (q == 0 && g < op.npw) {
-      const cplx<T> x = in[g];
-      const cplx<T> res = op.g2kin[g] * x + sgm * x + scale * col[op.g_col[g] * op.ldz + op.g_i3[g]] + sum;
-      out[g] = res;
-      if (out2) out2[g] = res;
-    }
-  };
-  if (pl.nst >= 3)
-    panel_pipeline<3>(op, pl, body);
-  else
-    panel_pipeline<2>(op, pl, body);
-}
-
 // Line-per-thread variant of pw_apply_cta for box lengths with a register
 // FFT (fftreg.cuh): each thread transforms a whole i3 column, i2 line or i1
 // row in registers.  PF planes are in flight per round; an i1 row is
@@ -359,37 +189,26 @@ __device__ void pw_apply_cta_lines(const PwView<T>& op, const int PF, const cplx
   const int nocc = (op.alpha_pv > 1e-14 || op.alpha_pv < -1e-14) ? op.nocc : 0;  // eps14, linear_op.f90:131
   const int ldz = op.ldz, pitch = op.pitch, psz = op.nr2 * op.pitch;
 
-  // The projectors: with a staging plan they stream through the idle plane
-  // buffers by asynchronous copies (panel_project / panel_gather);
-  // otherwise each warp takes one projection and streams its row from L2.
-  const int npan = op.nkb + nocc;
-  const long long plane_elems = (long long)PF * psz;
-  const PanelPlan<T> plp = panel_plan<T>(op, npan, planes, plane_elems, true);
-  const cplx<T>* src = in;
-  if (plp.ok) {
-    panel_project<T>(op, plp, in, bec);
-    src = plp.xs;
-  } else {
-    // <beta_i|psi> D_i and alpha_pv <evq_v|psi>, one warp per projection; the
-    // unrolled loop keeps eight loads of each lane in flight
-    for (int i = warp; i < npan; i += nwarp) {
-      const cplx<T>* pr = (i < op.nkb) ? op.vkb + (size_t)i * op.npwx : op.evq + (size_t)(i - op.nkb) * op.npwx;
-      cplx<T> acc = {0, 0};
+  // <beta_i|psi> D_i and alpha_pv <evq_v|psi>, one warp per projection; the
+  // unrolled loop keeps eight loads of each lane in flight (the projectors
+  // stream from L2)
+  for (int i = warp; i < op.nkb + nocc; i += nwarp) {
+    const cplx<T>* pr = (i < op.nkb) ? op.vkb + (size_t)i * op.npwx : op.evq + (size_t)(i - op.nkb) * op.npwx;
+    cplx<T> acc = {0, 0};
 #pragma unroll 8
-      for (int g = lane; g < op.npw; g += 32) cfma_conj(acc, pr[g], in[g]);
+    for (int g = lane; g < op.npw; g += 32) cfma_conj(acc, pr[g], in[g]);
 #pragma unroll
-      for (int o = 16; o > 0; o >>= 1) {
-        acc.re += __shfl_xor_sync(0xffffffffu, acc.re, o);
-        acc.im += __shfl_xor_sync(0xffffffffu, acc.im, o);
-      }
-      if (lane == 0) bec[i] = (i < op.nkb ? op.dvan[i] : (T)op.alpha_pv) * acc;
+    for (int o = 16; o > 0; o >>= 1) {
+      acc.re += __shfl_xor_sync(0xffffffffu, acc.re, o);
+      acc.im += __shfl_xor_sync(0xffffffffu, acc.im, o);
     }
+    if (lane == 0) bec[i] = (i < op.nkb ? op.dvan[i] : (T)op.alpha_pv) * acc;
   }
   for (int c = tid; c < op.ncol; c += nt) cpos[c] = op.col_pos[c];
   // the column store is not cleared: the inverse i3 pass reads only the
   // points that hold sphere values (zmask), and every later reader reads
   // points written earlier in the same apply
-  for (int g = tid; g < op.npw; g += nt) col[op.g_col[g] * ldz + op.g_i3[g]] = src[g];
+  for (int g = tid; g < op.npw; g += nt) col[op.g_col[g] * ldz + op.g_i3[g]] = in[g];
   __syncthreads();
 
   // Line e of a pass goes to thread e mod blockDim: lines fill whole warps
@@ -491,11 +310,6 @@ __device__ void pw_apply_cta_lines(const PwView<T>& op, const int PF, const cplx
   with_len<T>(op.nr3, [&](auto NN) { zpass(NN, MINUS{}); });
   __syncthreads();
 
-  const PanelPlan<T> plg = panel_plan<T>(op, npan, planes, plane_elems, false);
-  if (plg.ok) {
-    panel_gather<T>(op, plg, in, out, out2, sigma, bec, col);
-    return;
-  }
   const T scale = (T)(1.0 / (double)op.nnr);
   const cplx<T> sg = ccast<T>(sigma);
   for (int g = tid; g < op.npw; g += nt) {
