@@ -189,33 +189,50 @@ __device__ void pw_apply_cta_lines(const PwView<T>& op, const int PF, const cplx
   const int nocc = (op.alpha_pv > 1e-14 || op.alpha_pv < -1e-14) ? op.nocc : 0;  // eps14, linear_op.f90:131
   const int ldz = op.ldz, pitch = op.pitch, psz = op.nr2 * op.pitch;
 
-  // <beta_i|psi> D_i and alpha_pv <evq_v|psi>: each warp takes four projections
-  // at once (rows i0 + k nwarp), so every load of psi feeds four products and
-  // each lane keeps several rows' loads in flight (the projectors stream from L2)
-  const int npan = op.nkb + nocc;
-  for (int i0 = warp; i0 < npan; i0 += 4 * nwarp) {
-    const cplx<T>* pr[4];
+  // The projections <beta_i|psi> D_i and alpha_pv <evq_v|psi> stream their rows
+  // from L2.  FP32: each warp takes four projections at once (rows i0 + k nwarp),
+  // so every load of psi feeds four products and each lane keeps several rows'
+  // loads in flight (measured 7% faster per apply at 40^3); FP64 (FP64-pipe
+  // bound, where that form measured slower): one warp per projection.
+  if constexpr (sizeof(T) == 4) {
+    const int npan = op.nkb + nocc;
+    for (int i0 = warp; i0 < npan; i0 += 4 * nwarp) {
+      const cplx<T>* pr[4];
 #pragma unroll
-    for (int k = 0; k < 4; ++k) {
-      const int i = min(i0 + k * nwarp, npan - 1);  // rows past the end repeat the last one (discarded)
-      pr[k] = (i < op.nkb) ? op.vkb + (size_t)i * op.npwx : op.evq + (size_t)(i - op.nkb) * op.npwx;
-    }
-    cplx<T> acc[4] = {{0, 0}, {0, 0}, {0, 0}, {0, 0}};
+      for (int k = 0; k < 4; ++k) {
+        const int i = min(i0 + k * nwarp, npan - 1);  // rows past the end repeat the last one (discarded)
+        pr[k] = (i < op.nkb) ? op.vkb + (size_t)i * op.npwx : op.evq + (size_t)(i - op.nkb) * op.npwx;
+      }
+      cplx<T> acc[4] = {{0, 0}, {0, 0}, {0, 0}, {0, 0}};
 #pragma unroll 4
-    for (int g = lane; g < op.npw; g += 32) {
-      const cplx<T> x = in[g];
+      for (int g = lane; g < op.npw; g += 32) {
+        const cplx<T> x = in[g];
 #pragma unroll
-      for (int k = 0; k < 4; ++k) cfma_conj(acc[k], pr[k][g], x);
+        for (int k = 0; k < 4; ++k) cfma_conj(acc[k], pr[k][g], x);
+      }
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+          acc[k].re += __shfl_xor_sync(0xffffffffu, acc[k].re, o);
+          acc[k].im += __shfl_xor_sync(0xffffffffu, acc[k].im, o);
+        }
+        const int i = i0 + k * nwarp;
+        if (lane == 0 && i < npan) bec[i] = (i < op.nkb ? op.dvan[i] : (T)op.alpha_pv) * acc[k];
+      }
     }
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
+  } else {
+    for (int i = warp; i < op.nkb + nocc; i += nwarp) {
+      const cplx<T>* pr = (i < op.nkb) ? op.vkb + (size_t)i * op.npwx : op.evq + (size_t)(i - op.nkb) * op.npwx;
+      cplx<T> acc = {0, 0};
+#pragma unroll 8
+      for (int g = lane; g < op.npw; g += 32) cfma_conj(acc, pr[g], in[g]);
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) {
-        acc[k].re += __shfl_xor_sync(0xffffffffu, acc[k].re, o);
-        acc[k].im += __shfl_xor_sync(0xffffffffu, acc[k].im, o);
+        acc.re += __shfl_xor_sync(0xffffffffu, acc.re, o);
+        acc.im += __shfl_xor_sync(0xffffffffu, acc.im, o);
       }
-      const int i = i0 + k * nwarp;
-      if (lane == 0 && i < npan) bec[i] = (i < op.nkb ? op.dvan[i] : (T)op.alpha_pv) * acc[k];
+      if (lane == 0) bec[i] = (i < op.nkb ? op.dvan[i] : (T)op.alpha_pv) * acc;
     }
   }
   for (int c = tid; c < op.ncol; c += nt) cpos[c] = op.col_pos[c];
@@ -285,7 +302,7 @@ __device__ void pw_apply_cta_lines(const PwView<T>& op, const int PF, const cplx
   __syncthreads();
   for (int p0 = 0; p0 < op.nr3; p0 += PF) {
     const int np = min(PF, op.nr3 - p0);
-    {  // V_loc(r) of this round's planes (contiguous) into L1 while the i2 pass runs
+    if constexpr (sizeof(T) == 4) {  // V_loc(r) of this round's planes (contiguous) into L1 during the i2 pass
       const char* vb = reinterpret_cast<const char*>(op.vrs + (size_t)p0 * op.nr1 * op.nr2);
       const int lines = (int)(((size_t)np * op.nr1 * op.nr2 * sizeof(T) + 127) / 128);
       for (int q = tid; q < lines; q += nt) asm volatile("prefetch.global.L1 [%0];" ::"l"(vb + 128 * (size_t)q));
@@ -331,30 +348,43 @@ __device__ void pw_apply_cta_lines(const PwView<T>& op, const int PF, const cplx
 
   const T scale = (T)(1.0 / (double)op.nnr);
   const cplx<T> sg = ccast<T>(sigma);
-  // two plane waves per thread and pass, so each projector coefficient read
-  // from shared memory feeds two rows' loads in flight
-  for (int g = tid; g < op.npw; g += 2 * nt) {
-    const int gb = g + nt < op.npw ? g + nt : g;  // a missing second row repeats the first (not stored)
-    const cplx<T> xa = in[g], xb = in[gb];
-    cplx<T> ra = op.g2kin[g] * xa + sg * xa + scale * col[op.g_col[g] * ldz + op.g_i3[g]];
-    cplx<T> rb = op.g2kin[gb] * xb + sg * xb + scale * col[op.g_col[gb] * ldz + op.g_i3[gb]];
+  if constexpr (sizeof(T) == 4) {
+    // FP32: two plane waves per thread and pass, so each projector coefficient
+    // read from shared memory feeds two rows' loads in flight
+    for (int g = tid; g < op.npw; g += 2 * nt) {
+      const int gb = g + nt < op.npw ? g + nt : g;  // a missing second row repeats the first (not stored)
+      const cplx<T> xa = in[g], xb = in[gb];
+      cplx<T> ra = op.g2kin[g] * xa + sg * xa + scale * col[op.g_col[g] * ldz + op.g_i3[g]];
+      cplx<T> rb = op.g2kin[gb] * xb + sg * xb + scale * col[op.g_col[gb] * ldz + op.g_i3[gb]];
 #pragma unroll 4
-    for (int i = 0; i < op.nkb; ++i) {
-      const cplx<T> b = bec[i];
-      cfma(ra, op.vkb[(size_t)i * op.npwx + g], b);
-      cfma(rb, op.vkb[(size_t)i * op.npwx + gb], b);
-    }
+      for (int i = 0; i < op.nkb; ++i) {
+        const cplx<T> b = bec[i];
+        cfma(ra, op.vkb[(size_t)i * op.npwx + g], b);
+        cfma(rb, op.vkb[(size_t)i * op.npwx + gb], b);
+      }
 #pragma unroll 4
-    for (int v = 0; v < nocc; ++v) {
-      const cplx<T> b = bec[op.nkb + v];
-      cfma(ra, op.evq[(size_t)v * op.npwx + g], b);
-      cfma(rb, op.evq[(size_t)v * op.npwx + gb], b);
+      for (int v = 0; v < nocc; ++v) {
+        const cplx<T> b = bec[op.nkb + v];
+        cfma(ra, op.evq[(size_t)v * op.npwx + g], b);
+        cfma(rb, op.evq[(size_t)v * op.npwx + gb], b);
+      }
+      out[g] = ra;
+      if (out2) out2[g] = ra;
+      if (gb != g) {
+        out[gb] = rb;
+        if (out2) out2[gb] = rb;
+      }
     }
-    out[g] = ra;
-    if (out2) out2[g] = ra;
-    if (gb != g) {
-      out[gb] = rb;
-      if (out2) out2[gb] = rb;
+  } else {
+    for (int g = tid; g < op.npw; g += nt) {
+      const cplx<T> x = in[g];
+      cplx<T> r = op.g2kin[g] * x + sg * x + scale * col[op.g_col[g] * ldz + op.g_i3[g]];
+#pragma unroll 8
+      for (int i = 0; i < op.nkb; ++i) cfma(r, op.vkb[(size_t)i * op.npwx + g], bec[i]);
+#pragma unroll 8
+      for (int v = 0; v < nocc; ++v) cfma(r, op.evq[(size_t)v * op.npwx + g], bec[op.nkb + v]);
+      out[g] = r;
+      if (out2) out2[g] = r;
     }
   }
   __syncthreads();
