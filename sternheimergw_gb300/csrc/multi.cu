@@ -730,8 +730,13 @@ std::vector<PwShape> tune_candidates(sgw_operator* op) {
   const bool reg = fft_reg_supported<T>(v.nr1) && fft_reg_supported<T>(v.nr2) && fft_reg_supported<T>(v.nr3);
   for (int lines = reg ? 1 : 0; lines >= 0; --lines)
     for (int in_smem = 1; in_smem >= 0; --in_smem) {
-      std::vector<int> pfs = lines ? std::vector<int>{1, 2, 3, 4, 6, 8, 10, 12, 16, 20, 24, 32}
-                                   : std::vector<int>{1, 2, 4};
+      // line FFT: every plane count up to 32 (the counts that fill the i2 and
+      // i1 passes' thread rounds evenly differ from box to box)
+      std::vector<int> pfs;
+      if (lines)
+        for (int pf = 1; pf <= 32; ++pf) pfs.push_back(pf);
+      else
+        pfs = {1, 2, 4};
       for (int pf : pfs) {
         if (lines && pf > v.nr3) continue;
         const size_t need = small(pf) + (in_smem ? colb : 0);
