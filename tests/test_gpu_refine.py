@@ -104,7 +104,14 @@ def test_warm_start(c0_system, gpu_lib, precision):
     xw, ew, itw = sg.solve_batch(op, b1, sh, threshold=1e-12, precision=precision, x0=x0)
     assert (ec == 0).all() and (ew == 0).all()
     err = np.linalg.norm(xw - xc, axis=2) / np.linalg.norm(xc, axis=2)
-    # mixed: the seed is refined in FP64; the other shifts of both solves carry complex64 defects
-    assert err[:, 0].max() < 1e-8, err[:, 0].max()
-    assert err.max() < (1e-8 if precision == 0 else 1e-4), err.max()
+    assert err[:, 0].max() < 1e-8, err[:, 0].max()  # the seed (FP64-refined in mixed precision)
+    if precision == 0:
+        assert err.max() < 1e-8, err.max()
+    else:
+        # the other shifts of a mixed solve carry complex64 collinearity defects: the warm-started
+        # solution must be as close to the FP64 solution as the cold one
+        x64, _, _ = sg.solve_batch(op, b1, sh, threshold=1e-12)
+        ew64 = np.linalg.norm(xw - x64, axis=2) / np.linalg.norm(x64, axis=2)
+        ec64 = np.linalg.norm(xc - x64, axis=2) / np.linalg.norm(x64, axis=2)
+        assert ew64.max() <= 2 * ec64.max() + 1e-8, (ew64.max(), ec64.max())
     assert itw.sum() < itc.sum(), (itw, itc)
