@@ -168,28 +168,6 @@ struct ShiftRef {
   __device__ zcd& at(long long off, int idx) const { return base[off + (long long)idx * P + s]; }
 };
 
-// The shifts' coefficient vectors over the basis (u_i^sigma, x_inc^sigma) in
-// the element type of the solve: FP64 in the FP64 solve, FP32 in the FP32
-// rounds of the mixed form (their vectors are FP32 too); the scalar
-// recurrences (phi, theta, alpha^sigma, beta^sigma, Horner) and the window
-// accumulators stay FP64.  The FP32 elements use the first half of the same
-// [field][P] region (offsets in FP64-complex units, scaled).
-template <typename T> struct CoefOf { using type = zcd; };
-template <> struct CoefOf<float> { using type = zcf; };
-
-template <typename CT>
-struct ShiftVec {
-  CT* base;
-  int s, P;
-  static constexpr int kScale = (int)(sizeof(zcd) / sizeof(CT));
-  __device__ CT& at(long long off, int idx) const { return base[off * kScale + (long long)idx * P + s]; }
-};
-
-template <typename CT>
-__device__ __forceinline__ CT to_coef(zcd v) {
-  return CT{(decltype(CT{}.re))v.re, (decltype(CT{}.re))v.im};
-}
-
 // Scalar recurrences of one shifted system (FP64, one thread per shift).  The
 // vector updates that use them run either on coefficient vectors (mode 0) or
 // on explicit shift vectors (mode 1).
@@ -250,59 +228,48 @@ __device__ inline void shift_mr_scalars(const ShiftRef& sh, const CoefLayout& L,
 // coalesced accesses ([field][P] layout, shift fastest).
 
 // bicgstab.f90:641-662 at step j, before the seed's r update.
-template <typename CT>
-__device__ __forceinline__ void replay_bicg1_q(const ShiftRef& sh, const ShiftVec<CT>& sv, const CoefLayout& L,
-                                               const zcd* cr, int j, int q) {
-  const CT beta_s = to_coef<CT>(sh.at(L.o_scal, SC_BETA)), alpha_s = to_coef<CT>(sh.at(L.o_scal, SC_ALPHA));
-  const CT factor = to_coef<CT>(sh.at(L.o_scal, SC_F1));
+__device__ __forceinline__ void replay_bicg1_q(const ShiftRef& sh, const CoefLayout& L, const zcd* cr, int j, int q) {
+  const zcd beta_s = sh.at(L.o_scal, SC_BETA), alpha_s = sh.at(L.o_scal, SC_ALPHA), factor = sh.at(L.o_scal, SC_F1);
   const int D = L.D, Db = L.Db;
   const bool b = q < Db;
   for (int i = 0; i <= j; ++i) {  // L15: u_i = -beta u_i + factor r_i
-    CT& u = sv.at(L.o_us, i * D + q);
-    CT v = -beta_s * u;
-    if (b) v += factor * to_coef<CT>(cr[i * Db + q]);
+    zcd& u = sh.at(L.o_us, i * D + q);
+    zcd v = -beta_s * u;
+    if (b) v += factor * cr[i * Db + q];
     u = v;
   }
-  sv.at(L.o_xinc, q) += alpha_s * sv.at(L.o_us, q);                                             // L17
-  sv.at(L.o_us, (j + 1) * D + q) = b ? factor * to_coef<CT>(cr[j * Db + q]) : to_coef<CT>(zcd{0.0, 0.0});  // L19
+  sh.at(L.o_xinc, q) += alpha_s * sh.at(L.o_us, q);                                    // L17
+  sh.at(L.o_us, (j + 1) * D + q) = b ? factor * cr[j * Db + q] : zcd{0.0, 0.0};         // L19
 }
 
 // bicgstab.f90:692-696 after the seed's r update of step j.
-template <typename CT>
-__device__ __forceinline__ void replay_bicg2_q(const ShiftRef& sh, const ShiftVec<CT>& sv, const CoefLayout& L,
-                                               const zcd* cr, int j, int q) {
-  const CT factor = to_coef<CT>(sh.at(L.o_scal, SC_F2));
-  const CT inv_alpha = to_coef<CT>(zcd{1.0, 0.0} / sh.at(L.o_scal, SC_ALPHA));
-  const CT msig = to_coef<CT>(-sh.at(L.o_scal, SC_SIG));
+__device__ __forceinline__ void replay_bicg2_q(const ShiftRef& sh, const CoefLayout& L, const zcd* cr, int j, int q) {
+  const zcd factor = sh.at(L.o_scal, SC_F2);
+  const zcd inv_alpha = zcd{1.0, 0.0} / sh.at(L.o_scal, SC_ALPHA);
+  const zcd msig = -sh.at(L.o_scal, SC_SIG);
   const int D = L.D, Db = L.Db;
-  CT u = sv.at(L.o_us, (j + 1) * D + q);
-  if (q < Db) u += factor * to_coef<CT>(cr[j * Db + q]);
+  zcd u = sh.at(L.o_us, (j + 1) * D + q);
+  if (q < Db) u += factor * cr[j * Db + q];
   u = inv_alpha * u;
-  u += msig * sv.at(L.o_us, j * D + q);
-  sv.at(L.o_us, (j + 1) * D + q) = u;
+  u += msig * sh.at(L.o_us, j * D + q);
+  sh.at(L.o_us, (j + 1) * D + q) = u;
 }
 
 // bicgstab.f90:886-911 on coefficient vectors; cr holds the seed r_j after Gram-Schmidt.
-template <typename CT>
-__device__ __forceinline__ void replay_mr_q(const ShiftRef& sh, const ShiftVec<CT>& sv, const CoefLayout& L,
-                                            const zcd* cr, const SeedShared& ss, int q) {
+__device__ __forceinline__ void replay_mr_q(const ShiftRef& sh, const CoefLayout& L, const zcd* cr, const SeedShared& ss,
+                                            int q) {
   const int l = L.l, D = L.D, Db = L.Db;
   const bool b = q < Db;
-  CT x = sv.at(L.o_xinc, q);
-  CT u0 = sv.at(L.o_us, q);
-  if (b) x += to_coef<CT>(sh.at(L.o_gpp, 0) * cr[q]);
-  u0 += to_coef<CT>(-ss.gamma[l]) * sv.at(L.o_us, l * D + q);
+  zcd x = sh.at(L.o_xinc, q);
+  zcd u0 = sh.at(L.o_us, q);
+  if (b) x += sh.at(L.o_gpp, 0) * cr[q];
+  u0 += (-ss.gamma[l]) * sh.at(L.o_us, l * D + q);
   for (int jj = 1; jj <= l - 1; ++jj) {
-    u0 += to_coef<CT>(-ss.gamma[jj]) * sv.at(L.o_us, jj * D + q);
-    if (b) x += to_coef<CT>(sh.at(L.o_gpp, jj) * cr[jj * Db + q]);
+    u0 += (-ss.gamma[jj]) * sh.at(L.o_us, jj * D + q);
+    if (b) x += sh.at(L.o_gpp, jj) * cr[jj * Db + q];
   }
-  sv.at(L.o_xinc, q) = x;
-  sv.at(L.o_us, q) = to_coef<CT>(sh.at(L.o_scal, SC_F1)) * u0;  // L34: u_0 / psi
-}
-
-template <typename CT>
-__device__ __forceinline__ zcd from_coef(CT v) {
-  return zcd{(double)v.re, (double)v.im};
+  sh.at(L.o_xinc, q) = x;
+  sh.at(L.o_us, q) = sh.at(L.o_scal, SC_F1) * u0;  // L34: u_0 / psi
 }
 
 // Fold the finished outer iteration (basis block at kw) into the window
@@ -310,7 +277,6 @@ __device__ __forceinline__ zcd from_coef(CT v) {
 // e of the CTA-wide loop is (k, shift) for the old window part, then (q, shift)
 // for the new block; the carries Xd, Uc are updated by the shift's own thread
 // once every thread has read them.
-template <typename CT>
 __device__ __forceinline__ void replay_window_cta(zcd* C, const CoefLayout& L, int kw, int Sm1) {
   const int Db = L.Db;
   const long long n_old = (long long)kw * Sm1, n_new = (long long)Db * Sm1;
@@ -319,22 +285,20 @@ __device__ __forceinline__ void replay_window_cta(zcd* C, const CoefLayout& L, i
     const long long f = old ? e : e - n_old;
     const int s = (int)(f % Sm1), k = (int)(f / Sm1);
     const ShiftRef sh{C, s, L.P};
-    const ShiftVec<CT> sv{reinterpret_cast<CT*>(C), s, L.P};
     if (old) {
-      const zcd d = from_coef(sv.at(L.o_xinc, Db)), c = from_coef(sv.at(L.o_us, Db));
+      const zcd d = sh.at(L.o_xinc, Db), c = sh.at(L.o_us, Db);
       zcd& ub = sh.at(L.o_ub, k);
       sh.at(L.o_xa, k) += d * ub;
       ub = c * ub;
     } else {
-      sh.at(L.o_xa, kw + k) = from_coef(sv.at(L.o_xinc, k));
-      sh.at(L.o_ub, kw + k) = from_coef(sv.at(L.o_us, k));
+      sh.at(L.o_xa, kw + k) = sh.at(L.o_xinc, k);
+      sh.at(L.o_ub, kw + k) = sh.at(L.o_us, k);
     }
   }
   __syncthreads();
   for (int s = threadIdx.x; s < Sm1; s += blockDim.x) {
     const ShiftRef sh{C, s, L.P};
-    const ShiftVec<CT> sv{reinterpret_cast<CT*>(C), s, L.P};
-    const zcd d = from_coef(sv.at(L.o_xinc, Db)), c = from_coef(sv.at(L.o_us, Db));
+    const zcd d = sh.at(L.o_xinc, Db), c = sh.at(L.o_us, Db);
     zcd& Uc = sh.at(L.o_scal, SC_UC);
     sh.at(L.o_scal, SC_XD) += d * Uc;
     Uc = c * Uc;
@@ -585,7 +549,6 @@ __device__ void solve_one(const SolverArgs<T>& a, const ApplyT& A, int rhs, int 
   cplx<T>* gbuf = A.scratch(sm, gelems);
   const int grows = max(1, gelems / a.P);
   const bool track = Sm1 > 0 && !explicit_mode;
-  using CT = typename CoefOf<T>::type;
 
   cplx<T>* V = a.ws_vec + (size_t)slot * a.vec_stride;
   cplx<T>* U = V;
@@ -680,10 +643,10 @@ __device__ void solve_one(const SolverArgs<T>& a, const ApplyT& A, int rhs, int 
         (v <= l ? cr : cu)[e - (v <= l ? 0 : (l + 1) * Db)] = zcd{one, 0.0};
       }
       for (int s = tid; s < Sm1; s += nt) {
-        const ShiftVec<CT> sv{reinterpret_cast<CT*>(C), s, L.P};
+        const ShiftRef sh{C, s, L.P};
         for (int q = 0; q < L.D; ++q) {
-          sv.at(L.o_us, q) = to_coef<CT>(zcd{q == Db ? 1.0 : 0.0, 0.0});
-          sv.at(L.o_xinc, q) = to_coef<CT>(zcd{0.0, 0.0});
+          sh.at(L.o_us, q) = zcd{q == Db ? 1.0 : 0.0, 0.0};
+          sh.at(L.o_xinc, q) = zcd{0.0, 0.0};
         }
       }
     }
@@ -713,9 +676,7 @@ __device__ void solve_one(const SolverArgs<T>& a, const ApplyT& A, int rhs, int 
       for (int s = tid; s < Sm1; s += nt) shift_bicg_scalars(ShiftRef{C, s, L.P}, L, alpha, beta, alpha_old);
       __syncthreads();
       if (track) {
-        for (int e = tid; e < L.D * Sm1; e += nt)
-          replay_bicg1_q<CT>(ShiftRef{C, e % Sm1, L.P}, ShiftVec<CT>{reinterpret_cast<CT*>(C), e % Sm1, L.P}, L, cr, j,
-                             e / Sm1);
+        for (int e = tid; e < L.D * Sm1; e += nt) replay_bicg1_q(ShiftRef{C, e % Sm1, L.P}, L, cr, j, e / Sm1);
         __syncthreads();
       }
       if (explicit_mode) {  // L15-L19 on the shift vectors, all shifts at once
@@ -746,9 +707,7 @@ __device__ void solve_one(const SolverArgs<T>& a, const ApplyT& A, int rhs, int 
       v_axpy(X, alpha, UV(0), n);
       __syncthreads();
       if (track)
-        for (int e = tid; e < L.D * Sm1; e += nt)
-          replay_bicg2_q<CT>(ShiftRef{C, e % Sm1, L.P}, ShiftVec<CT>{reinterpret_cast<CT*>(C), e % Sm1, L.P}, L, cr, j,
-                             e / Sm1);
+        for (int e = tid; e < L.D * Sm1; e += nt) replay_bicg2_q(ShiftRef{C, e % Sm1, L.P}, L, cr, j, e / Sm1);
       if (explicit_mode)  // L26
         for (long long e = tid; e < (long long)Sm1 * n; e += nt) {
           const int s = (int)(e / n), g = (int)(e - (long long)s * n);
@@ -808,9 +767,7 @@ __device__ void solve_one(const SolverArgs<T>& a, const ApplyT& A, int rhs, int 
       for (int s = tid; s < Sm1; s += nt) shift_mr_scalars(ShiftRef{C, s, L.P}, L, ss);
       __syncthreads();
       if (track) {
-        for (int e = tid; e < L.D * Sm1; e += nt)
-          replay_mr_q<CT>(ShiftRef{C, e % Sm1, L.P}, ShiftVec<CT>{reinterpret_cast<CT*>(C), e % Sm1, L.P}, L, cr, ss,
-                          e / Sm1);
+        for (int e = tid; e < L.D * Sm1; e += nt) replay_mr_q(ShiftRef{C, e % Sm1, L.P}, L, cr, ss, e / Sm1);
         __syncthreads();
       }
       if (explicit_mode) {  // L28-L34
@@ -837,7 +794,7 @@ __device__ void solve_one(const SolverArgs<T>& a, const ApplyT& A, int rhs, int 
       __syncthreads();
     }
     if (track) {
-      replay_window_cta<CT>(C, L, kw, Sm1);
+      replay_window_cta(C, L, kw, Sm1);
       kw += Db;
     }
     __syncthreads();
