@@ -47,7 +47,7 @@ METRIC = "Sternheimer solves/sec: batched mixed vs plain FP64, same GPU, W err â
 # on 152 right-hand sides of this workload (dram__bytes_read.sum +
 # dram__bytes_write.sum over the same count's algorithmic bytes); roofline.traffic
 # is this ratio times the algorithmic bytes of the timed launches.
-NCU_TRAFFIC_OVER_ALGORITHMIC = {"fp32": 2.78, "fp64": 13.7}
+NCU_TRAFFIC_OVER_ALGORITHMIC = {"fp32": 2.87, "fp64": 14.0}
 CONV_TOL = 1e-6          # a pair is a solve when its true relative residual is at most this
 CONV_SAMPLE = 32         # right-hand sides of the convergence sample (all 70 shifts each)
 WORKLOAD = "sc8 a=10.26 25Ry 40^3 npw=2293 nkb=32 nocc=16 npert=113 nfreq=35 (S=70) lmax=4 thr=1e-10"
@@ -391,12 +391,17 @@ def w_error_imag_axis():
     xo, _, _ = O.bicgstab_many(O.PlaneWaveOperator(s), B.reshape(npert * nocc, -1), sh, threshold=THRESHOLD)
     Wo = linter_ref.w_from_chi(linter_ref.chi_matrix(B, xo.reshape(npert, nocc, sh.shape[1], -1), f), v)
     so = sigma_ref.sigma_diag(s, Wo, v, y, mu, bands)
+
+    def werr(Wx):
+        return float(np.max(np.linalg.norm(Wx - Wo, axis=(1, 2)) / np.linalg.norm(Wo, axis=(1, 2))))
+
+    vs_oracle = {"fp64": werr(W64), "mixed": werr(WM)}
     sig_err = {"fp64_vs_oracle": float(np.max(np.abs(sig["fp64"] - so) / np.abs(so))),
                "mixed_vs_oracle": float(np.max(np.abs(sig["mixed"] - so) / np.abs(so))),
                "mixed_vs_fp64": float(np.max(np.abs(sig["mixed"] - sig["fp64"]) / np.abs(sig["fp64"]))),
                "sigma_ry": [float(v.real) for v in so],
                "system": "imaginary-axis system, 4 bands, Sigma_c(mu) diagonal, W and G in the named precision"}
-    return norm, elem, int(max(e64.max(), em.max())), sig_err
+    return norm, elem, int(max(e64.max(), em.max())), sig_err, vs_oracle
 
 
 def run_c3(steps=2, warmup=1, sequential=True):
@@ -638,14 +643,15 @@ def run_gpu(args, rank, world):
                 "0.1 eV broadening stay unconverged in both precisions (nearly singular shifted matrices)",
     }
     del xr64_d, xrm_d
-    w_norm, w_elem, w_ierr, sig = w_error_imag_axis()
-    # The mixed form's accuracy gate is W (the metric's "W err <= 1e-6"): its shifted solutions
+    w_norm, w_elem, w_ierr, sig, w_oracle = w_error_imag_axis()
+    # The mixed form's accuracy gate is W (the metric's "W err <= 1e-6", against the GPU FP64
+    # solve and against the oracle's W): its shifted solutions
     # carry complex64 collinearity defects (true residuals ~1e-5 on ill-conditioned shifts) that
     # average out in W.  With the gate met on the imaginary-axis system and on every defined
     # frequency of the workload, a mixed pair counts as a solve when the FP64 solve of the same
     # pair converged; otherwise only its own true residual counts.
     wd = w_c1["plain"]["mixed_vs_fp64"]
-    w_gate = bool(w_norm <= 1e-6 and (wd is None or wd <= 1e-6))
+    w_gate = bool(w_norm <= 1e-6 and w_oracle["mixed"] <= 1e-6 and (wd is None or wd <= 1e-6))
     frac_value = frac64 if w_gate else fracm
     value = world * frac_value * pairs / (ms_m * 1e-3)
 
@@ -721,6 +727,11 @@ def run_gpu(args, rank, world):
         sample = min(nrhs, 32 * (os.cpu_count() or 1))
         cpu = cpu_reference(s, bb, sigma, sample, os.cpu_count() or 1, count_rows=rows)
         cpu_frac = cpu["converged_fraction"]
+        # the same restatement on one core, on a few right-hand sides (pairs/s for comparison)
+        from oracle import oracle as O
+        t1 = time.time()
+        O.bicgstab_many(O.PlaneWaveOperator(s), bb[:4], sigma[:4], lmax=LMAX, threshold=THRESHOLD, nthreads=1)
+        one_core_pps = 4 * S / (time.time() - t1)
         # the GPU solutions against the oracle's own solutions of the sample
         xo = cpu["x"]
         sub = cpu["rows_in_sample"]
@@ -771,6 +782,7 @@ def run_gpu(args, rank, world):
             "w_err": {"normwise_max_over_freq": w_norm, "elementwise_max": w_elem, "ierr_max": w_ierr,
                       "system": "imaginary-axis system (fcc 20^3, 8 perturbations x 16 frequencies i[0,50] eV), "
                                 "every shifted system converged; mixed vs FP64",
+                      "vs_oracle_normwise_max": w_oracle,
                       "ok": bool(w_norm <= 1e-6)},
             "w_err_workload": w_c1,
             "sigma_err": sig,
@@ -814,6 +826,7 @@ def run_gpu(args, rank, world):
             "uneven_batch": c3,
             "cpu_baseline": {"value": cpu["value"], "unit": "solves/s", "cores": os.cpu_count() or 1, "kind": "port",
                              "pairs_per_s": cpu["pairs_per_s"], "converged_fraction": cpu_frac,
+                             "one_core_pairs_per_s": one_core_pps,
                              "sample": f"{sample} of {nrhs} right-hand sides x {S} shifts, {cpu['seconds']:.1f}s; "
                                        f"converged fraction from {cpu['rows_in_sample'].size} of them"},
             "gpu_launches": int(pm["launches"]),

@@ -61,20 +61,47 @@ __host__ __device__ inline int pw_smem_small(const PwView<T>& op, int ng) {
   return op.nr1 + op.nr2 + op.nr3 + op.nkb + op.nocc + pw_cpos_units(op) + ng * op.nr2 * op.pitch;
 }
 
-// CTA-wide sum of a double2 partial; result broadcast to every thread.
-__device__ __forceinline__ zcd cta_sum(zcd v, zcd* red) {
+// CTA-wide sums of per-thread partials, the FP64 result broadcast to every
+// thread.  Each warp reduces its lanes with shuffles (in the partials' own
+// precision); lane w < nw of every warp then loads warp w's sum and a
+// butterfly over those lanes gives all threads the same total, in the same
+// order.  FP64 issues at about 1/60 of the FP32 rate on GB300: the butterfly
+// costs log2(nw) FP64 adds per warp where a loop over the warp sums in every
+// thread costs nw.
+__device__ __forceinline__ zcd cta_sum_warps(zcd v, zcd* red) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  __syncthreads();  // red[] may still be read by a previous call
+  if (lane == 0) red[warp] = v;
+  __syncthreads();
+  int p = 1;
+  while (p < nw) p <<= 1;
+  zcd t = lane < nw ? red[lane] : zcd{0.0, 0.0};
+  for (int o = p >> 1; o > 0; o >>= 1) {
+    t.re += __shfl_xor_sync(0xffffffffu, t.re, o);
+    t.im += __shfl_xor_sync(0xffffffffu, t.im, o);
+  }
+  t.re = __shfl_sync(0xffffffffu, t.re, 0);
+  t.im = __shfl_sync(0xffffffffu, t.im, 0);
+  return t;
+}
+
+__device__ __forceinline__ zcd cta_sum(zcd v, zcd* red) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
     v.re += __shfl_xor_sync(0xffffffffu, v.re, o);
     v.im += __shfl_xor_sync(0xffffffffu, v.im, o);
   }
-  __syncthreads();  // red[] may still be read by a previous call
-  if (lane == 0) red[warp] = v;
-  __syncthreads();
-  zcd s = {0.0, 0.0};
-  for (int w = 0; w < nw; ++w) s += red[w];
-  return s;
+  return cta_sum_warps(v, red);
+}
+
+// FP32 partials (the FP32 Krylov rounds): the in-warp steps stay in FP32.
+__device__ __forceinline__ zcd cta_sum(zcf v, zcd* red) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    v.re += __shfl_xor_sync(0xffffffffu, v.re, o);
+    v.im += __shfl_xor_sync(0xffffffffu, v.im, o);
+  }
+  return cta_sum_warps(ccast<double>(v), red);
 }
 
 // Unconjugated dot (ZDOTU) of two length-n vectors, CTA-wide, FP64 result.
@@ -82,7 +109,7 @@ template <typename T>
 __device__ zcd cta_dotu(const cplx<T>* x, const cplx<T>* y, int n, zcd* red) {
   cplx<T> p = {0, 0};
   for (int i = threadIdx.x; i < n; i += blockDim.x) cfma(p, x[i], y[i]);
-  return cta_sum(ccast<double>(p), red);
+  return cta_sum(p, red);
 }
 
 // sum |x|^2 (for the 2-norm), CTA-wide
@@ -90,7 +117,7 @@ template <typename T>
 __device__ double cta_nrm2sq(const cplx<T>* x, int n, zcd* red) {
   T p = 0;
   for (int i = threadIdx.x; i < n; i += blockDim.x) p += abs2(x[i]);
-  return cta_sum(zcd{(double)p, 0.0}, red).re;
+  return cta_sum(cplx<T>{p, (T)0}, red).re;
 }
 
 // out = (H + sigma + alpha_pv P_v) in   (and out2 = the same, if non-null).

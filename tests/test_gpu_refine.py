@@ -108,10 +108,15 @@ def test_warm_start(c0_system, gpu_lib, precision):
     if precision == 0:
         assert err.max() < 1e-8, err.max()
     else:
-        # the other shifts of a mixed solve carry complex64 collinearity defects: the warm-started
-        # solution must be as close to the FP64 solution as the cold one
+        # the other shifts of a mixed solve carry complex64 collinearity defects, and a warm start
+        # keeps those of its starting point (it corrects with the seed's residual): the warm-started
+        # solution may be off the FP64 solution by the start's error plus one cold solve's error
         x64, _, _ = sg.solve_batch(op, b1, sh, threshold=1e-12)
-        ew64 = np.linalg.norm(xw - x64, axis=2) / np.linalg.norm(x64, axis=2)
-        ec64 = np.linalg.norm(xc - x64, axis=2) / np.linalg.norm(x64, axis=2)
-        assert ew64.max() <= 2 * ec64.max() + 1e-8, (ew64.max(), ec64.max())
+        x64_0, _, _ = sg.solve_batch(op, b0, sh, threshold=1e-12)
+        nrm = np.linalg.norm(x64, axis=2)
+        ew64 = np.linalg.norm(xw - x64, axis=2) / nrm
+        ec64 = np.linalg.norm(xc - x64, axis=2) / nrm
+        e0 = np.linalg.norm(x0 - x64_0, axis=2) / nrm
+        assert ew64.max() <= e0.max() + ec64.max() + 1e-8, (ew64.max(), e0.max(), ec64.max())
+        assert ew64.max() < 1e-4, ew64.max()
     assert itw.sum() < itc.sum(), (itw, itc)
