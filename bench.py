@@ -537,6 +537,28 @@ def run_caller(args):
     return out
 
 
+def host_link_probe(torch, nbytes=1 << 30):
+    """Plain copies of 1 GiB each way between page-locked host memory and the
+    device (CUDA events), taken before anything else runs: the host link of
+    this box, against which the end-to-end copies can be read."""
+    h = torch.empty(nbytes, dtype=torch.uint8).pin_memory()
+    d = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+    out = {}
+    for name, dst, src in (("d2h_gbs", h, d), ("h2d_gbs", d, h)):
+        best = 1e30
+        for _ in range(3):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            e0.record()
+            dst.copy_(src, non_blocking=True)
+            e1.record()
+            e1.synchronize()
+            best = min(best, e0.elapsed_time(e1))
+        out[name] = nbytes / (best * 1e-3) / 1e9
+    del h, d
+    return out
+
+
 def run_gpu(args, rank, world):
     import torch
     import torch.distributed as dist
@@ -547,6 +569,7 @@ def run_gpu(args, rank, world):
     dev = int(os.environ.get("LOCAL_RANK", 0))
     torch.cuda.set_device(dev)
     _capi.lib(build_if_missing=False)
+    link_start = host_link_probe(torch)
     holder = {}
 
     def make_op(system):
@@ -793,6 +816,7 @@ def run_gpu(args, rank, world):
                     "host_buffers": "sgw_host_alloc (page-locked, transparent huge pages)",
                     "output_huge_page_fraction": None if x_huge is None else x_huge / x_h.nbytes,
                     "host_link_plain_copy": link,
+                    "host_link_at_start": link_start,
                     "copy_in_ms_all": [c[0] for c in e2e["mixed"]["copies"]],
                     "copy_out_ms_all": [c[1] for c in e2e["mixed"]["copies"]]},
             "roofline": {"bound": "fp32", "achieved": ach32, "peak": peak32, "unit": "TFLOP/s",
