@@ -75,8 +75,29 @@ struct SeedShared {
   zcd gamma_p[kMaxL + 1];
   zcd gamma_pp[kMaxL + 1];
   zcd red[32];
+  zcd bc[2];  // cta_sum_then broadcast
+  // FP32 copies of the gammas for the FP32 vector updates (no conversion per element)
+  zcf gamma32[kMaxL + 1];
+  zcf gamma_p32[kMaxL + 1];
+  zcf gamma_pp32[kMaxL + 1];
   int flag;
 };
+
+// A seed gamma in the vector precision: FP32 copies in the FP32 solve.
+template <typename T>
+__device__ __forceinline__ cplx<T> seed_coef(const zcd* a64, const zcf* a32, int i) {
+  if constexpr (sizeof(T) == 4)
+    return a32[i];
+  else
+    return a64[i];
+}
+
+// The reference's convergence test on the seed residual (|r|_2 < threshold,
+// bicgstab.f90:278-301), the square root taken by one thread.
+template <typename T>
+__device__ __forceinline__ bool below_threshold(const cplx<T>* r, int n, SeedShared& ss, double thr) {
+  return cta_nrm2sq_then(r, n, ss.red, ss.bc, [&](zcd t) { return zcd{sqrt(t.re) < thr ? 1.0 : 0.0, 0.0}; }).re != 0.0;
+}
 
 #define SGW_MUIDX(j, i) ((j) * ((j) + 1) / 2 + (i))
 #define SGW_TAUIDX(j, i) ((j) * ((j) + 1) / 2 + (i))
@@ -89,7 +110,7 @@ struct CoefLayout {
     D = 2 * l + 3;
     Db = 2 * l + 2;
     long long o = 0;
-    o_scal = o; o += 10LL * P;                      // the SC_* scalars
+    o_scal = o; o += 11LL * P;                      // the SC_* scalars
     o_mu = o; o += (long long)(l * (l + 1) / 2) * P;
     o_us = o; o += (long long)(l + 1) * D * P;
     o_xinc = o; o += (long long)D * P;
@@ -105,7 +126,7 @@ struct CoefLayout {
   }
 };
 
-enum { SC_PHIOLD = 0, SC_PHI, SC_THETA, SC_SIG, SC_ALPHA, SC_UC, SC_XD, SC_BETA, SC_F1, SC_F2 };
+enum { SC_PHIOLD = 0, SC_PHI, SC_THETA, SC_SIG, SC_ALPHA, SC_UC, SC_XD, SC_BETA, SC_F1, SC_F2, SC_IALPHA };
 
 // --- operator adaptors -------------------------------------------------------
 
@@ -172,16 +193,20 @@ struct ShiftRef {
 // vector updates that use them run either on coefficient vectors (mode 0) or
 // on explicit shift vectors (mode 1).
 
-// bicgstab.f90:625-638 and :655-657 at BiCG step j.
-__device__ inline void shift_bicg_scalars(const ShiftRef& sh, const CoefLayout& L, zcd alpha, zcd beta, zcd alpha_old) {
+// bicgstab.f90:625-638 and :655-657 at BiCG step j; ab = alpha beta / alpha_old
+// of the seed (the same for every shift).  FP64 divisions cost tens of FP64
+// instructions each on GB300, so each quotient is formed once.
+__device__ inline void shift_bicg_scalars(const ShiftRef& sh, const CoefLayout& L, zcd alpha, zcd beta, zcd ab) {
   const zcd one = {1.0, 0.0};
   zcd& inv_phi_old = sh.at(L.o_scal, SC_PHIOLD);
   zcd& inv_phi = sh.at(L.o_scal, SC_PHI);
   const zcd sig = sh.at(L.o_scal, SC_SIG);
-  const zcd inv_phi_new = inv_phi / (one + alpha * sig + alpha * beta / alpha_old * (inv_phi / inv_phi_old - one));
   const zcd ratio = inv_phi / inv_phi_old;
+  const zcd inv_phi_new = inv_phi / (one + alpha * sig + ab * (ratio - one));
   sh.at(L.o_scal, SC_BETA) = ratio * ratio * beta;
-  sh.at(L.o_scal, SC_ALPHA) = (inv_phi_new / inv_phi) * alpha;
+  const zcd alpha_s = (inv_phi_new / inv_phi) * alpha;
+  sh.at(L.o_scal, SC_ALPHA) = alpha_s;
+  sh.at(L.o_scal, SC_IALPHA) = one / alpha_s;  // read by every coefficient of the L26 replay
   sh.at(L.o_scal, SC_F1) = sh.at(L.o_scal, SC_THETA) * inv_phi;  // 1/(theta phi) of L15/L19
   inv_phi_old = inv_phi;
   inv_phi = inv_phi_new;
@@ -196,7 +221,8 @@ __device__ inline void replay_horner(const ShiftRef& sh, const CoefLayout& L, co
   psi = -sigma * sh.at(L.o_gs, 1) + zcd{1.0, 0.0};
   for (int ii = 1; ii <= l - 1; ++ii)
     for (int jj = l - 1; jj >= ii; --jj) sh.at(L.o_gs, jj) = -sigma * sh.at(L.o_gs, jj + 1) + sh.at(L.o_gs, jj);
-  for (int jj = 1; jj <= l; ++jj) sh.at(L.o_gs, jj) = -sh.at(L.o_gs, jj) / psi;
+  const zcd minv_psi = -(zcd{1.0, 0.0} / psi);  // one division for the l quotients
+  for (int jj = 1; jj <= l; ++jj) sh.at(L.o_gs, jj) = sh.at(L.o_gs, jj) * minv_psi;
 }
 
 // bicgstab.f90:854-884: MR scalars of one shift.  Leaves the x-update factors
@@ -245,7 +271,7 @@ __device__ __forceinline__ void replay_bicg1_q(const ShiftRef& sh, const CoefLay
 // bicgstab.f90:692-696 after the seed's r update of step j.
 __device__ __forceinline__ void replay_bicg2_q(const ShiftRef& sh, const CoefLayout& L, const zcd* cr, int j, int q) {
   const zcd factor = sh.at(L.o_scal, SC_F2);
-  const zcd inv_alpha = zcd{1.0, 0.0} / sh.at(L.o_scal, SC_ALPHA);
+  const zcd inv_alpha = sh.at(L.o_scal, SC_IALPHA);
   const zcd msig = -sh.at(L.o_scal, SC_SIG);
   const int D = L.D, Db = L.Db;
   zcd u = sh.at(L.o_us, (j + 1) * D + q);
@@ -655,8 +681,8 @@ __device__ void solve_one(const SolverArgs<T>& a, const ApplyT& A, int rhs, int 
     // ---- bicg_part (bicgstab.f90:520-702) ----
     rho_old = -omega * rho_old;
     for (int j = 0; j < l; ++j) {
-      const zcd rho = cta_dotu(RV(j), TR0, n, ss.red);
-      beta = alpha * rho / rho_old;
+      zcd rho;
+      beta = cta_dotu_then(RV(j), TR0, n, ss.red, ss.bc, [&](zcd r) { return alpha * r / rho_old; }, &rho);
       rho_old = rho;
       {
         const cplx<T> mb = ccast<T>(-beta);
@@ -672,8 +698,11 @@ __device__ void solve_one(const SolverArgs<T>& a, const ApplyT& A, int rhs, int 
       A.apply(UV(j), UV(j + 1), track ? W + (size_t)(kw + 2 + 2 * j) * npwx : nullptr, sigma_seed, sm, col);
       if (track)
         for (int q = tid; q < Db; q += nt) cu[(j + 1) * Db + q] = zcd{q == 2 + 2 * j ? 1.0 : 0.0, 0.0};
-      alpha = rho / cta_dotu(UV(j + 1), TR0, n, ss.red);
-      for (int s = tid; s < Sm1; s += nt) shift_bicg_scalars(ShiftRef{C, s, L.P}, L, alpha, beta, alpha_old);
+      alpha = cta_dotu_then(UV(j + 1), TR0, n, ss.red, ss.bc, [&](zcd d) { return rho / d; });
+      {
+        const zcd ab = alpha * beta / alpha_old;
+        for (int s = tid; s < Sm1; s += nt) shift_bicg_scalars(ShiftRef{C, s, L.P}, L, alpha, beta, ab);
+      }
       __syncthreads();
       if (track) {
         for (int e = tid; e < L.D * Sm1; e += nt) replay_bicg1_q(ShiftRef{C, e % Sm1, L.P}, L, cr, j, e / Sm1);
@@ -712,18 +741,18 @@ __device__ void solve_one(const SolverArgs<T>& a, const ApplyT& A, int rhs, int 
         for (long long e = tid; e < (long long)Sm1 * n; e += nt) {
           const int s = (int)(e / n), g = (int)(e - (long long)s * n);
           cplx<T> u = USV(s, j + 1)[g] + ccast<T>(SCAL(s, SC_F2)) * RV(j)[g];
-          u = ccast<T>(zcd{1.0, 0.0} / SCAL(s, SC_ALPHA)) * u;
+          u = ccast<T>(SCAL(s, SC_IALPHA)) * u;
           USV(s, j + 1)[g] = u + ccast<T>(-SCAL(s, SC_SIG)) * USV(s, j)[g];
         }
       __syncthreads();
     }
-    conv = sqrt(cta_nrm2sq(RV(0), n, ss.red)) < a.threshold;
+    conv = below_threshold(RV(0), n, ss, a.threshold);
 
     if (!conv) {
       // ---- mr_part (bicgstab.f90:708-931) ----
       for (int jj = 1; jj <= l; ++jj) {
         for (int ii = 1; ii <= jj - 1; ++ii) {
-          const zcd tau = cta_dotu(RV(jj), RV(ii), n, ss.red) / ss.nu[ii];
+          const zcd tau = cta_dotu_then(RV(jj), RV(ii), n, ss.red, ss.bc, [&](zcd d) { return d / ss.nu[ii]; });
           if (tid == 0) ss.tau[SGW_TAUIDX(jj, ii)] = tau;
           v_axpy(RV(jj), -tau, RV(ii), n);
           if (track)
@@ -731,10 +760,11 @@ __device__ void solve_one(const SolverArgs<T>& a, const ApplyT& A, int rhs, int 
           __syncthreads();
         }
         const zcd nu = cta_dotu(RV(jj), RV(jj), n, ss.red);
-        const zcd gp = cta_dotu(RV(0), RV(jj), n, ss.red) / nu;
+        const zcd gp = cta_dotu_then(RV(0), RV(jj), n, ss.red, ss.bc, [&](zcd d) { return d / nu; });
         if (tid == 0) {
           ss.nu[jj] = nu;
           ss.gamma_p[jj] = gp;
+          ss.gamma_p32[jj] = ccast<float>(gp);
         }
         __syncthreads();
       }
@@ -750,16 +780,18 @@ __device__ void solve_one(const SolverArgs<T>& a, const ApplyT& A, int rhs, int 
           for (int ii = jj + 1; ii <= l - 1; ++ii) gsum = gsum + ss.tau[SGW_TAUIDX(ii, jj)] * ss.gamma[ii + 1];
           ss.gamma_pp[jj] = gsum;
         }
+        for (int jj = 1; jj <= l; ++jj) ss.gamma32[jj] = ccast<float>(ss.gamma[jj]);
+        for (int jj = 1; jj <= l - 1; ++jj) ss.gamma_pp32[jj] = ccast<float>(ss.gamma_pp[jj]);
       }
       __syncthreads();
       omega = ss.gamma[l];
       for (int g = tid; g < n; g += nt) {  // L14-L17
         cplx<T> x = X[g], u0 = UV(0)[g];
-        x += ccast<T>(ss.gamma[1]) * RV(0)[g];
-        u0 += ccast<T>(-ss.gamma[l]) * UV(l)[g];
+        x += seed_coef<T>(ss.gamma, ss.gamma32, 1) * RV(0)[g];
+        u0 += -seed_coef<T>(ss.gamma, ss.gamma32, l) * UV(l)[g];
         for (int jj = 1; jj <= l - 1; ++jj) {
-          u0 += ccast<T>(-ss.gamma[jj]) * UV(jj)[g];
-          x += ccast<T>(ss.gamma_pp[jj]) * RV(jj)[g];
+          u0 += -seed_coef<T>(ss.gamma, ss.gamma32, jj) * UV(jj)[g];
+          x += seed_coef<T>(ss.gamma_pp, ss.gamma_pp32, jj) * RV(jj)[g];
         }
         X[g] = x;
         UV(0)[g] = u0;
@@ -788,7 +820,7 @@ __device__ void solve_one(const SolverArgs<T>& a, const ApplyT& A, int rhs, int 
       }
       for (int g = tid; g < n; g += nt) {  // delayed L32
         cplx<T> r0 = RV(0)[g];
-        for (int jj = 1; jj <= l; ++jj) r0 += ccast<T>(-ss.gamma_p[jj]) * RV(jj)[g];
+        for (int jj = 1; jj <= l; ++jj) r0 += -seed_coef<T>(ss.gamma_p, ss.gamma_p32, jj) * RV(jj)[g];
         RV(0)[g] = r0;
       }
       __syncthreads();
@@ -799,7 +831,7 @@ __device__ void solve_one(const SolverArgs<T>& a, const ApplyT& A, int rhs, int 
     }
     __syncthreads();
     if (conv) break;
-    conv = sqrt(cta_nrm2sq(RV(0), n, ss.red)) < a.threshold;
+    conv = below_threshold(RV(0), n, ss, a.threshold);
     if (conv) break;
   }
 

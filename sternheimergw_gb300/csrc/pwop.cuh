@@ -104,6 +104,40 @@ __device__ __forceinline__ zcd cta_sum(zcf v, zcd* red) {
   return cta_sum_warps(ccast<double>(v), red);
 }
 
+// A CTA-wide sum whose FP64 total feeds one scalar function f (a quotient, a
+// square root, a test), evaluated by a single thread and broadcast through
+// shared memory: bc[0] = total, bc[1] = f(total).  FP64 divisions and square
+// roots cost tens of FP64 instructions, and every warp evaluating the same
+// scalar multiplies that by the warp count.  One barrier more than cta_sum.
+template <typename CT, class F>
+__device__ __forceinline__ zcd cta_sum_then(CT v, zcd* red, zcd* bc, F f, zcd* total) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    v.re += __shfl_xor_sync(0xffffffffu, v.re, o);
+    v.im += __shfl_xor_sync(0xffffffffu, v.im, o);
+  }
+  __syncthreads();  // red[] and bc[] may still be read by a previous call
+  if (lane == 0) red[warp] = ccast<double>(v);
+  __syncthreads();
+  if (warp == 0) {
+    int p = 1;
+    while (p < nw) p <<= 1;
+    zcd t = lane < nw ? red[lane] : zcd{0.0, 0.0};
+    for (int o = p >> 1; o > 0; o >>= 1) {
+      t.re += __shfl_xor_sync(0xffffffffu, t.re, o);
+      t.im += __shfl_xor_sync(0xffffffffu, t.im, o);
+    }
+    if (lane == 0) {
+      bc[0] = t;
+      bc[1] = f(t);
+    }
+  }
+  __syncthreads();
+  if (total) *total = bc[0];
+  return bc[1];
+}
+
 // Unconjugated dot (ZDOTU) of two length-n vectors, CTA-wide, FP64 result.
 template <typename T>
 __device__ zcd cta_dotu(const cplx<T>* x, const cplx<T>* y, int n, zcd* red) {
@@ -118,6 +152,21 @@ __device__ double cta_nrm2sq(const cplx<T>* x, int n, zcd* red) {
   T p = 0;
   for (int i = threadIdx.x; i < n; i += blockDim.x) p += abs2(x[i]);
   return cta_sum(cplx<T>{p, (T)0}, red).re;
+}
+
+// cta_dotu / cta_nrm2sq with the total passed through f (cta_sum_then).
+template <typename T, class F>
+__device__ zcd cta_dotu_then(const cplx<T>* x, const cplx<T>* y, int n, zcd* red, zcd* bc, F f,
+                             zcd* total = nullptr) {
+  cplx<T> p = {0, 0};
+  for (int i = threadIdx.x; i < n; i += blockDim.x) cfma(p, x[i], y[i]);
+  return cta_sum_then(p, red, bc, f, total);
+}
+template <typename T, class F>
+__device__ zcd cta_nrm2sq_then(const cplx<T>* x, int n, zcd* red, zcd* bc, F f) {
+  T p = 0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) p += abs2(x[i]);
+  return cta_sum_then(cplx<T>{p, (T)0}, red, bc, f, nullptr);
 }
 
 // out = (H + sigma + alpha_pv P_v) in   (and out2 = the same, if non-null).
