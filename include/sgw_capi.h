@@ -538,7 +538,8 @@ sgw_status sgw_last_timing(sgw_operator* op, double* ms, int64_t* launches);
  * kernels), 4 = the last sgw_chi, 5 = the last sgw_vjp; 6 = the host-to-device
  * and 7 = the device-to-host copies of the last host-memory sgw_solve_batch
  * (0 after a device-memory call); 8 = the last sgw_screened_coulomb, 9 = the
- * last sgw_sigma_diag. */
+ * last sgw_sigma_diag; 10 = the FP32 seed-residual updates of the mixed
+ * rounds after the first. */
 sgw_status sgw_kernel_timing(sgw_operator* op, int32_t kernel, double* ms, int64_t* launches);
 
 /* One-line description of the last error on this thread. */

@@ -87,7 +87,9 @@ struct Workspace {
 
 // Kernel kinds timed with CUDA events on the operator's stream.
 // Timed spans of the last call, by kind: the solve kernels (0-2), the caller-side
-// kernels (3-5) and the host-path copies of sgw_solve_batch (6 in, 7 out).
+// kernels (3-5), the host-path copies of sgw_solve_batch (6 in, 7 out), the
+// screened Coulomb and self-energy kernels (8, 9) and the FP32 residual update
+// of the mixed rounds (10).
 enum KernelKind {
   K_MSBICG_F64 = 0,
   K_MSBICG_F32 = 1,
@@ -99,7 +101,8 @@ enum KernelKind {
   K_COPY_OUT = 7,
   K_SCREEN = 8,
   K_SIGMA = 9,
-  K_NUM = 10
+  K_RESIDUAL_F32 = 10,
+  K_NUM = 11
 };
 constexpr int kMaxTimedLaunches = 64;
 

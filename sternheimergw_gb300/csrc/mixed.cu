@@ -75,7 +75,8 @@ sgw_status solve_mixed(sgw_operator* op, const BatchDev& b, int refine_max, doub
     SGW_CK(cudaStreamSynchronize(op->stream));
     if (h_active == 0) {
       if (round == 0) {  // every right-hand side is zero: so is every solution
-        mx_accumulate<<<R * S, tb, 0, op->stream>>>(R, S, n, npwx, y32, x, b.ldx, b.ldr, Z, scale, active, true, bad);
+        mx_accumulate<<<R * S, tb, 0, op->stream>>>(R, S, n, npwx, y32, x, b.ldx, b.ldr, Z, scale, active, true, bad,
+                                                    nullptr);
         op->last_launches += 1;
       }
       all_done = true;
@@ -90,8 +91,10 @@ sgw_status solve_mixed(sgw_operator* op, const BatchDev& b, int refine_max, doub
                 npwx, (long long)S * npwx, b.ierr, iters_round, active, zeta, round > 0 ? 1 : 0};
     if ((s = run_msbicg<float>(op, bf)) != SGW_OK) return s;
     if (copied) SGW_CK(cudaStreamWaitEvent(op->stream, op->ev_copied, 0));  // the last copy still reads x
+    // from round 1 on the seed's increment (FP32) goes to r32 (free once the round is solved) for the
+    // residual update below
     mx_accumulate<<<R * S, tb, 0, op->stream>>>(R, S, n, npwx, y32, x, b.ldx, b.ldr, Z, scale, active, round == 0,
-                                                  bad);
+                                                  bad, round > 0 ? r32 : nullptr);
     mx_update_z<<<(R * S + tb - 1) / tb, tb, 0, op->stream>>>(R, S, Z, zeta, active, iters_total, iters_round);
     op->last_launches += 2;
     // x may be final now: copy it out while the FP64 residual decides.  A round
@@ -105,6 +108,29 @@ sgw_status solve_mixed(sgw_operator* op, const BatchDev& b, int refine_max, doub
       SGW_CK(cudaMemcpyAsync(out->host, x, out->bytes, cudaMemcpyDeviceToHost, op->copy_stream));
       SGW_CK(cudaEventRecord(op->ev_copied, op->copy_stream));
       copied = true;
+    }
+    if (round > 0) {
+      // r -= A(sigma_1) c with the round's increment c, in FP32 (mx_residual_update)
+      s = with_applier<float>(op, [&](auto A, size_t smem) -> sgw_status {
+        auto kern = mx_residual_update<decltype(A)>;
+        const long long colsz = (op->kind == 1 && !op->shape32.col_in_smem) ? col_elems<float>(op) : 0;
+        const int grid = std::min(R, op->num_sms);
+        if (colsz) {
+          sgw_status s2 = op->ws32.col.ensure(sizeof(zcf) * colsz * grid);
+          if (s2 != SGW_OK) return s2;
+        }
+        SGW_CK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        const int t = ktime_begin(op, K_RESIDUAL_F32);
+        kern<<<grid, CtaThreads<float>::v, smem, op->stream>>>(A, R, n, b.sigma, b.lds, r32, npwx, y32,
+                                                              (long long)S * npwx, r64, npwx, active,
+                                                              op->ws32.col.as<zcf>(), colsz);
+        ktime_end(op, t);
+        SGW_CK(cudaGetLastError());
+        op->last_launches += 1;
+        return SGW_OK;
+      });
+      if (s != SGW_OK) return s;
+      continue;
     }
     // FP64 true residual of the seed system
     s = with_applier<double>(op, [&](auto A, size_t smem) -> sgw_status {

@@ -58,6 +58,22 @@ struct ResEntry {
   const int* active;
 };
 
+// FP32 seed-residual update of one system (mixed rounds after the first):
+// r -= A(sigma_1) c, c = the round's increment of x_1 (see mx_residual_update)
+template <class ApplyT>
+struct ResUpdEntry {
+  ApplyT A;
+  int n;
+  const zcd* sigma;
+  long long lds;
+  const zcf* c;  // [nrhs][ldrr]
+  zcf* ac;       // A c: the round's seed rows of y32
+  long long ldac;
+  zcd* r;
+  long long ldrr;
+  const int* active;
+};
+
 constexpr size_t kConstBytes = 60 * 1024;
 __constant__ __align__(16) unsigned char c_entries[kConstBytes];
 
@@ -132,6 +148,39 @@ __global__ void __launch_bounds__(THREADS, 1)
   }
 }
 
+// r -= A(sigma_1) c in FP32 for the active right-hand sides of every system
+template <class ApplyT, int THREADS>
+__global__ void __launch_bounds__(THREADS, 1)
+    residual_update_multi_kernel(const MultiItem* items, int nitems, int* counter, zcf* col_global,
+                                 long long col_slot, unsigned long long* sys_end) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ int s_item;
+  const ResUpdEntry<ApplyT>* E = reinterpret_cast<const ResUpdEntry<ApplyT>*>(c_entries);
+  zcf* sm = reinterpret_cast<zcf*>(smem_raw);
+  int cur = -1;
+  while (true) {
+    if (threadIdx.x == 0) s_item = atomicAdd(counter, 1);
+    __syncthreads();
+    const int it = s_item;
+    __syncthreads();
+    if (it >= nitems) break;
+    const MultiItem m = items[it];
+    const ResUpdEntry<ApplyT>& e = E[m.sys];
+    if (!e.active[m.rhs]) continue;
+    if (m.sys != cur) {
+      e.A.setup(sm);
+      cur = m.sys;
+    }
+    zcf* col = e.A.col_in_smem ? sm + e.A.smem_small() : col_global + (size_t)blockIdx.x * col_slot;
+    zcf* out = e.ac + (size_t)m.rhs * e.ldac;
+    e.A.apply(e.c + (size_t)m.rhs * e.ldrr, out, nullptr, e.sigma[(size_t)m.rhs * e.lds], sm, col);
+    zcd* rr = e.r + (size_t)m.rhs * e.ldrr;
+    for (int g = threadIdx.x; g < e.n; g += blockDim.x) rr[g] = rr[g] - zcd{(double)out[g].re, (double)out[g].im};
+    __syncthreads();
+    if (threadIdx.x == 0) atomicMax(sys_end + m.sys, gtimer());
+  }
+}
+
 // Floating-point work of one operator apply of a system (FFT lines actually
 // needed, V_loc multiply, projectors): the cost model of the item order.
 double apply_cost(const PwView<double>& v) {
@@ -168,7 +217,7 @@ struct sgw_multi {
   cudaEvent_t ev_caller = nullptr;  // orders the plan's stream after the caller's
   int num_sms = 0, nslots = 0;
   // solve stage (FP64 solve for precision 0, FP32 rounds for precision 1) and FP64 residual stage
-  std::vector<sgw::MultiGroup> solve_groups, res_groups;
+  std::vector<sgw::MultiGroup> solve_groups, res_groups, upd_groups;
   sgw::DevBuf vec, coef, col, col64, counters, stamps;
   // mixed precision, per system: r64, r32, y32, Z, zeta, scale, bnorm, active, iters_round, nactive
   sgw::DevBuf mixed;
@@ -431,6 +480,99 @@ sgw_status launch_res_stage(sgw_multi* P, int& counter_idx) {
   return SGW_OK;
 }
 
+// FP32 seed-residual update groups (mixed rounds after the first)
+sgw_status build_upd_groups(sgw_multi* P) {
+  const int ns = P->nsys;
+  sgw_status s;
+  P->upd_groups.clear();
+  for (int variant = 0; variant < 2; ++variant) {
+    const bool lines = variant == 0;
+    std::vector<int> sys;
+    for (int i = 0; i < ns; ++i)
+      if (pwshape<float>(P->ops[i]).lines == lines) sys.push_back(i);
+    if (sys.empty()) continue;
+    MultiGroup g;
+    g.lines = lines;
+    std::vector<MultiItem> items;
+    for (int i : sys)
+      for (int r = 0; r < P->d[i].nrhs; ++r) items.push_back(MultiItem{i, r});
+    g.nitems = (int)items.size();
+    if ((s = g.items.upload(items.data(), std::max<size_t>(items.size(), 1))) != SGW_OK) return s;
+    auto build = [&](auto tag) -> sgw_status {
+      using AT = decltype(tag);
+      using E = ResUpdEntry<AT>;
+      if (sizeof(E) * ns > kConstBytes) {
+        set_error("too many systems for one launch");
+        return SGW_ERR_UNSUPPORTED;
+      }
+      std::vector<E> img(ns);
+      std::memset(static_cast<void*>(img.data()), 0, sizeof(E) * ns);
+      for (int i : sys) {
+        const PwShape& sh = pwshape<float>(P->ops[i]);
+        const sgw_batch_desc& d = P->d[i];
+        const long long npwx = P->ops[i]->npwx;
+        img[i].A = AT{view_of<float>(P->ops[i]), sh.col_in_smem, sh.ng};
+        img[i].n = P->ops[i]->n;
+        img[i].sigma = reinterpret_cast<const zcd*>(d.sigma);
+        img[i].lds = d.lds;
+        img[i].c = P->ms[i].r32;
+        img[i].ac = P->ms[i].y32;
+        img[i].ldac = (long long)d.num_shift * npwx;
+        img[i].r = P->ms[i].r64;
+        img[i].ldrr = npwx;
+        img[i].active = P->ms[i].active;
+        g.smem = std::max(g.smem, sh.smem);
+      }
+      g.entry_bytes = sizeof(E) * ns;
+      return g.entries.upload(reinterpret_cast<unsigned char*>(img.data()), g.entry_bytes);
+    };
+    s = lines ? build(PwA<float, true>{}) : build(PwA<float, false>{});
+    if (s != SGW_OK) return s;
+    P->upd_groups.push_back(std::move(g));
+  }
+  return SGW_OK;
+}
+
+sgw_status launch_upd_stage(sgw_multi* P, int& counter_idx) {
+  for (MultiGroup& g : P->upd_groups) {
+    int* counter = P->counters.as<int>() + counter_idx++;
+    SGW_CK(cudaMemsetAsync(counter, 0, sizeof(int), P->stream));
+    SGW_CK(cudaMemcpyToSymbolAsync(c_entries, g.entries.p, g.entry_bytes, 0, cudaMemcpyDeviceToDevice, P->stream));
+    constexpr int NT = CtaThreads<float>::v;
+    const int grid = std::max(1, std::min(P->num_sms, g.nitems));
+    unsigned long long* sys_end = P->stamps.as<unsigned long long>() + 1;
+    long long col_slot = 0;
+    for (int i = 0; i < P->nsys; ++i)
+      if (!pwshape<float>(P->ops[i]).col_in_smem) col_slot = std::max(col_slot, col_elems<float>(P->ops[i]));
+    if (g.lines) {
+      auto k = residual_update_multi_kernel<PwA<float, true>, NT>;
+      k<<<grid, NT, g.smem, P->stream>>>(g.items.as<MultiItem>(), g.nitems, counter, P->col.as<zcf>(), col_slot,
+                                          sys_end);
+    } else {
+      auto k = residual_update_multi_kernel<PwA<float, false>, NT>;
+      k<<<grid, NT, g.smem, P->stream>>>(g.items.as<MultiItem>(), g.nitems, counter, P->col.as<zcf>(), col_slot,
+                                          sys_end);
+    }
+    SGW_CK(cudaGetLastError());
+    P->launches += 1;
+  }
+  return SGW_OK;
+}
+
+sgw_status set_upd_attrs(std::vector<MultiGroup>& groups) {
+  constexpr int NT = CtaThreads<float>::v;
+  for (MultiGroup& g : groups) {
+    if (g.lines) {
+      SGW_CK(cudaFuncSetAttribute(residual_update_multi_kernel<PwA<float, true>, NT>,
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)g.smem));
+    } else {
+      SGW_CK(cudaFuncSetAttribute(residual_update_multi_kernel<PwA<float, false>, NT>,
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)g.smem));
+    }
+  }
+  return SGW_OK;
+}
+
 template <typename T>
 sgw_status set_smem_attrs(std::vector<MultiGroup>& groups) {
   constexpr int NT = CtaThreads<T>::v;
@@ -502,11 +644,13 @@ sgw_status enqueue(sgw_multi* P) {
       const int R = d.nrhs, S = d.num_shift, n = P->ops[i]->n, npwx = P->ops[i]->npwx;
       if (R == 0) continue;
       mx_accumulate<<<R * S, tb, 0, P->stream>>>(R, S, n, npwx, m.y32, reinterpret_cast<zcd*>(d.xx), d.ldx, d.ldr,
-                                                 m.Z, m.scale, m.active, round == 0, m.bad);
+                                                 m.Z, m.scale, m.active, round == 0, m.bad,
+                                                 round > 0 ? m.r32 : nullptr);
       mx_update_z<<<(R * S + tb - 1) / tb, tb, 0, P->stream>>>(R, S, m.Z, m.zeta, m.active, d.iters, m.iters_round);
       P->launches += 2;
     }
-    if ((s = launch_res_stage(P, ci)) != SGW_OK) return s;
+    // round 0: FP64 b - A x; later rounds: r -= A c in FP32
+    if ((s = round == 0 ? launch_res_stage(P, ci) : launch_upd_stage(P, ci)) != SGW_OK) return s;
   }
   for (int i = 0; i < ns; ++i) {
     const sgw_batch_desc& d = P->d[i];
@@ -647,6 +791,8 @@ sgw_status multi_create(int nsys, sgw_operator* const* ops, const sgw_batch_desc
     if ((s = set_smem_attrs<float>(P->solve_groups)) != SGW_OK) return fail(s);
     if ((s = build_res_groups(P)) != SGW_OK) return fail(s);
     if ((s = set_res_attrs(P->res_groups)) != SGW_OK) return fail(s);
+    if ((s = build_upd_groups(P)) != SGW_OK) return fail(s);
+    if ((s = set_upd_attrs(P->upd_groups)) != SGW_OK) return fail(s);
   }
   if (o.use_graph) {
     std::lock_guard<std::mutex> lk(g_const_mutex);
@@ -874,7 +1020,7 @@ sgw_status sgw_multi_destroy(sgw_multi* plan) {
   if (plan->stream) cudaStreamSynchronize(plan->stream);
   if (plan->gexec) cudaGraphExecDestroy(plan->gexec);
   if (plan->graph) cudaGraphDestroy(plan->graph);
-  for (auto* gs : {&plan->solve_groups, &plan->res_groups})
+  for (auto* gs : {&plan->solve_groups, &plan->res_groups, &plan->upd_groups})
     for (auto& g : *gs) {
       g.entries.release();
       g.entries_tc.release();

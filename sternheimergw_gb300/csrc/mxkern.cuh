@@ -53,8 +53,8 @@ __global__ void mx_normalise(int nrhs, int n, int npwx, const zcd* r, long long 
 // thread issues the loads of kAccUnroll elements before its first store.
 constexpr int kAccUnroll = 4;
 template <bool kF32>
-__device__ __forceinline__ void acc_row(const zcd f, const zcf* __restrict__ yr, zcd* __restrict__ xr, int n,
-                                        bool first, bool& nonfinite) {
+__device__ __forceinline__ void acc_row(const zcd f, const zcf* __restrict__ yr, zcd* __restrict__ xr,
+                                        zcf* __restrict__ crow, int n, bool first, bool& nonfinite) {
   const int nt = blockDim.x;
   const zcf f32 = zcf{(float)f.re, (float)f.im};
   for (int g0 = threadIdx.x; g0 < n; g0 += kAccUnroll * nt) {
@@ -77,9 +77,11 @@ __device__ __forceinline__ void acc_row(const zcd f, const zcf* __restrict__ yr,
           const zcf c = f32 * yv[u];
           nonfinite |= !(isfinite(c.re) && isfinite(c.im));
           add = zcd{(double)c.re, (double)c.im};
+          if (crow) crow[g] = c;
         } else {
           add = f * zcd{(double)yv[u].re, (double)yv[u].im};
           nonfinite |= !(isfinite(add.re) && isfinite(add.im));
+          if (crow) crow[g] = zcf{(float)add.re, (float)add.im};
         }
         xr[g] = first ? add : xv[u] + add;
       }
@@ -87,9 +89,11 @@ __device__ __forceinline__ void acc_row(const zcd f, const zcf* __restrict__ yr,
   }
 }
 
+// cseed (optional, [nrhs][npwx]): receives the increment of the seed shift in
+// FP32, for the residual update of mx_residual_update.
 __global__ void mx_accumulate(int nrhs, int S, int n, int npwx, const zcf* __restrict__ y, zcd* __restrict__ x,
                               long long ldx, long long ldr, const zcd* __restrict__ Z, const double* __restrict__ scale,
-                              const int* __restrict__ active, bool first, int* bad) {
+                              const int* __restrict__ active, bool first, int* bad, zcf* __restrict__ cseed) {
   const long long row = blockIdx.x;
   if (row >= (long long)nrhs * S) return;
   const int rhs = (int)(row / S), s = (int)(row - (long long)rhs * S);
@@ -103,11 +107,12 @@ __global__ void mx_accumulate(int nrhs, int S, int n, int npwx, const zcf* __res
   const double fa = fmax(fabs(f.re), fabs(f.im));
   // |f| in [1e-20, 1e20]: f y stays a normal FP32 number for |y| up to 1e18
   const bool f32 = fa == 0.0 || (fa >= 1e-20 && fa <= 1e20);
+  zcf* crow = (cseed && s == 0) ? cseed + (size_t)rhs * npwx : nullptr;
   bool nonfinite = false;
   if (f32)
-    acc_row<true>(f, y + (size_t)row * npwx, xr, n, first, nonfinite);
+    acc_row<true>(f, y + (size_t)row * npwx, xr, crow, n, first, nonfinite);
   else
-    acc_row<false>(f, y + (size_t)row * npwx, xr, n, first, nonfinite);
+    acc_row<false>(f, y + (size_t)row * npwx, xr, crow, n, first, nonfinite);
   if (__syncthreads_or(nonfinite) && threadIdx.x == 0) bad[rhs] = 1;
 }
 
@@ -147,6 +152,33 @@ __global__ void __launch_bounds__(CtaThreads<double>::v, 1)
     A.apply(x + (size_t)rhs * ldr, out, nullptr, sigma[(size_t)rhs * lds], sm, col);
     const zcd* b = bb + (size_t)rhs * ldb;
     for (int g = threadIdx.x; g < n; g += blockDim.x) out[g] = b[g] - out[g];
+    __syncthreads();
+  }
+}
+
+// r -= A(sigma_1) c in FP32 for active right-hand sides, one CTA each: the
+// seed residual after a correction round, updated from the previous round's
+// FP64 residual by the increment c that the round added to x_1 (b - A (x + c)
+// = r - A c, exactly).  After round 0 |c| is ~1e-5 |x| or less, so the FP32
+// apply's rounding (~1e-7 relative to A c) leaves an error of order 1e-12 |b|
+// in r - far below the 1e-9 refinement target - at 1/14 of the cost of an
+// FP64 apply of the whole x_1.  The round-0 residual is always the FP64
+// b - A x (mx_seed_residual).  ac: per-rhs FP32 scratch for A c.
+template <class ApplyT>
+__global__ void __launch_bounds__(CtaThreads<float>::v, 1)
+    mx_residual_update(ApplyT A, int nrhs, int n, const zcd* sigma, long long lds, const zcf* c, long long ldc,
+                       zcf* ac, long long ldac, zcd* r, long long ldr, const int* active, zcf* col_global,
+                       long long col_slot) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  zcf* sm = reinterpret_cast<zcf*>(smem_raw);
+  zcf* col = A.col_in_smem ? sm + A.smem_small() : col_global + (size_t)blockIdx.x * col_slot;
+  A.setup(sm);
+  for (int rhs = blockIdx.x; rhs < nrhs; rhs += gridDim.x) {
+    if (!active[rhs]) continue;
+    zcf* out = ac + (size_t)rhs * ldac;
+    A.apply(c + (size_t)rhs * ldc, out, nullptr, sigma[(size_t)rhs * lds], sm, col);
+    zcd* rr = r + (size_t)rhs * ldr;
+    for (int g = threadIdx.x; g < n; g += blockDim.x) rr[g] = rr[g] - zcd{(double)out[g].re, (double)out[g].im};
     __syncthreads();
   }
 }
