@@ -160,7 +160,8 @@ CallScope::~CallScope() {
 
 // Sum the per-kernel event pairs of the finished solve (stream already synchronised).
 void collect_kernel_times(sgw_operator* op) {
-  for (int k : {K_MSBICG_F64, K_MSBICG_F32, K_RESIDUAL_F64, K_COPY_IN, K_COPY_OUT}) {  // rhs/chi/vjp keep their own
+  // the kinds timed through the event pool; rhs/chi/vjp/screen/sigma keep their own
+  for (int k : {K_MSBICG_F64, K_MSBICG_F32, K_RESIDUAL_F64, K_COPY_IN, K_COPY_OUT, K_RESIDUAL_F32}) {
     op->kernel_ms[k] = 0.0;
     op->kernel_launches[k] = 0;
   }

@@ -115,3 +115,29 @@ def test_multishift_c1_reduced(c1_system, gpu_lib):
     ok = res <= 1e-8
     err = np.linalg.norm(x - xo, axis=2) / np.linalg.norm(xo, axis=2)
     assert err[ok].max() < 1e-5, err[ok].max()
+
+
+def test_mixed_c1_reduced_seed_residual(c1_system, gpu_lib):
+    """Mixed precision on 8 right-hand sides of the production system: the seed
+    solution's true residual, recomputed in FP64 by the oracle's apply, is at
+    most the 1e-9 refinement target (the residual after round 0 is an FP64
+    b - A x; later rounds update it with an FP32 apply of the round's increment,
+    whose rounding stays ~1e-12 |b|); the seed agrees with the oracle's
+    solution to the oracle's own accuracy."""
+    import sternheimergw_gb300 as sg
+    from oracle import linter_ref
+    from oracle import oracle as O
+    from sternheimergw_gb300 import linter
+    s, f = c1_system
+    bb = np.concatenate([linter_ref.coulomb_rhs(s, 2)[:4], linter_ref.coulomb_rhs(s, 3)[:4]])
+    sh1 = linter.coulomb_shifts(s, f)
+    sh = np.concatenate([sh1[:4], sh1[:4]])
+    x, ierr, iters = sg.solve_batch(sg.PlaneWaveOperator(s), bb, sh, threshold=1e-10, precision=1)
+    assert (ierr == 0).all() and (iters > 0).all()
+    oop = O.PlaneWaveOperator(s)
+    res = O.true_residuals(oop, bb, sh[:, :1], x[:, :1])[:, 0]
+    assert res.max() <= 1e-9, res.max()
+    xo, ierro, _ = O.bicgstab_many(oop, bb, sh[:, :1], threshold=1e-10)
+    assert (ierro == 0).all()
+    seed_err = np.linalg.norm(x[:, 0] - xo[:, 0], axis=1) / np.linalg.norm(xo[:, 0], axis=1)
+    assert seed_err.max() < 1e-8, seed_err

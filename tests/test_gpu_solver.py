@@ -198,6 +198,12 @@ def test_mixed_c0(c0):
     x64, ierr64, _ = sg.solve_batch(op, bb, sh, threshold=1e-10)
     xm, ierr, iters = sg.solve_batch(op, bb, sh, threshold=1e-10, precision=1)
     assert (ierr == 0).all() and (iters > 0).all()
+    # per-call kernel timings: the FP64 residual of round 0 and the FP32 updates of later rounds,
+    # counted afresh on every call
+    n_upd = op.kernel_timing(10)[1]
+    assert op.kernel_timing(2)[1] == 1 and n_upd >= 1
+    sg.solve_batch(op, bb, sh, threshold=1e-10, precision=1)
+    assert op.kernel_timing(10)[1] == n_upd and op.kernel_timing(2)[1] == 1
     for r in range(bb.shape[0]):
         res = op.apply(sh[r, 0], xm[r, 0]) - bb[r]
         assert np.linalg.norm(res) / np.linalg.norm(bb[r]) <= 1e-9
