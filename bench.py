@@ -623,11 +623,8 @@ def run_gpu(args, rank, world):
     nocc = s["nocc"]
 
     # end to end through the C ABI with page-locked host buffers from sgw_host_alloc
-    # (transparent huge pages): the mixed path (headline) and the plain FP64 drop-in.
-    # Measured right after the device-resident steps, before the host-side checks:
-    # on these hosts, copies into a registered buffer slowed to a few GB/s after the
-    # checker's OpenMP work and the accuracy runs (a host effect: fresh page-locked
-    # buffers and the device were unaffected); solves/s follow once the converged
+    # (transparent huge pages): the mixed path (headline) and the plain FP64 drop-in,
+    # right after the device-resident steps; solves/s follow once the converged
     # fractions are known.
     bb_h = sg.host_array(bb.shape)
     bb_h[...] = bb

@@ -129,6 +129,23 @@ static sgw_status init_common(sgw_operator* op) {
   SGW_CK(cudaEventCreate(&op->lev0));
   SGW_CK(cudaEventCreate(&op->lev1));
   for (int i = 0; i < 2 * kMaxTimedLaunches; ++i) SGW_CK(cudaEventCreate(&op->kev[i]));
+  SGW_CK(cudaHostAlloc(reinterpret_cast<void**>(&op->h_count), sizeof(int), cudaHostAllocMapped));
+  SGW_CK(cudaHostGetDevicePointer(reinterpret_cast<void**>(&op->d_count_alias), op->h_count, 0));
+  return SGW_OK;
+}
+
+static __global__ void publish_count(const int* src, int* dst) {
+  *reinterpret_cast<volatile int*>(dst) = *src;
+  __threadfence_system();
+}
+
+sgw_status read_count(sgw_operator* op, const int* dev, int* out) {
+  *reinterpret_cast<volatile int*>(op->h_count) = -1;
+  publish_count<<<1, 1, 0, op->stream>>>(dev, op->d_count_alias);
+  SGW_CK(cudaGetLastError());
+  op->last_launches += 1;
+  SGW_CK(cudaStreamSynchronize(op->stream));
+  *out = *reinterpret_cast<volatile int*>(op->h_count);
   return SGW_OK;
 }
 
@@ -719,13 +736,19 @@ static sgw_status host_alloc(size_t bytes, void** ptr) {
     p = reinterpret_cast<char*>(a);
   }
   madvise(p, len, MADV_HUGEPAGE);  // advisory: base pages remain if THP is off
-  std::memset(p, 0, len);          // populate before pinning
+  // Populate with a non-zero pattern, pin, then zero.  Buffers populated with
+  // zeros before cudaHostRegister were measured to copy at 3-18 GB/s on these
+  // hosts (from the start, or after a while), on huge and on base pages alike,
+  // while the same buffers populated with a non-zero pattern copied at 193 GB/s
+  // out and 211 GB/s in throughout - also after host work and large solves.
+  std::memset(p, 0x5a, len);
   const cudaError_t e = cudaHostRegister(p, len, cudaHostRegisterPortable);
   if (e != cudaSuccess) {
     munmap(p, len);
     set_error(std::string("cudaHostRegister failed: ") + cudaGetErrorString(e));
     return SGW_ERR_CUDA;
   }
+  std::memset(p, 0, len);
   {
     std::lock_guard<std::mutex> g(g_host_mu);
     g_host_bufs[p] = len;
@@ -804,6 +827,7 @@ sgw_status sgw_operator_destroy(sgw_operator* op) {
   if (op->ev_caller) cudaEventDestroy(op->ev_caller);
   if (op->copy_stream) cudaStreamDestroy(op->copy_stream);
   if (op->stream) cudaStreamDestroy(op->stream);
+  if (op->h_count) cudaFreeHost(op->h_count);
   delete op;
   return SGW_OK;
 }

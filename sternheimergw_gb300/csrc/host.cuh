@@ -121,6 +121,9 @@ struct sgw_operator {
   cudaStream_t copy_stream = nullptr;                 // host-path result copies overlapped with the solve
   cudaEvent_t ev_acc = nullptr, ev_copied = nullptr;  // its hand-offs (no timing)
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  // page-locked, device-mapped host ints: counts read back between rounds (read_count)
+  int* h_count = nullptr;
+  int* d_count_alias = nullptr;
   cudaEvent_t lev0 = nullptr, lev1 = nullptr;  // sgw_coulomb_rhs / sgw_chi timing
   double last_ms = 0.0;
   long long last_launches = 0;
@@ -206,6 +209,11 @@ class CallScope {
 // Sum the per-kernel event pairs of the last call into kernel_ms / kernel_launches
 // (the handle's stream must be synchronised).
 void collect_kernel_times(sgw_operator* op);
+// A device int, read on the host after the work queued on op->stream: one
+// thread stores it into the operator's page-locked, device-mapped host int and
+// the stream is synchronised.  No copy engine is involved, so the read does not
+// queue behind a large result copy in flight on the copy stream.
+sgw_status read_count(sgw_operator* op, const int* dev, int* out);
 // `stream` waits for the work queued so far on `caller` (event `ev` is reused).
 sgw_status order_after(cudaStream_t stream, cudaStream_t caller, cudaEvent_t ev);
 

@@ -71,8 +71,7 @@ sgw_status solve_mixed(sgw_operator* op, const BatchDev& b, int refine_max, doub
                                            refine_thr, active, nactive);
     op->last_launches += 1;
     int h_active = 0;
-    SGW_CK(cudaMemcpyAsync(&h_active, nactive, sizeof(int), cudaMemcpyDeviceToHost, op->stream));
-    SGW_CK(cudaStreamSynchronize(op->stream));
+    if ((s = read_count(op, nactive, &h_active)) != SGW_OK) return s;
     if (h_active == 0) {
       if (round == 0) {  // every right-hand side is zero: so is every solution
         mx_accumulate<<<R * S, tb, 0, op->stream>>>(R, S, n, npwx, y32, x, b.ldx, b.ldr, Z, scale, active, true, bad,

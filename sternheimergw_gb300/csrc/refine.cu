@@ -272,8 +272,7 @@ static sgw_status refine_rounds(sgw_operator* op, const BatchDev& b, const Batch
                                            pick ? nullptr : o.resid, bad);
     op->last_launches += 1;
     int h_active = 0;
-    SGW_CK(cudaMemcpyAsync(&h_active, nactive, sizeof(int), cudaMemcpyDeviceToHost, op->stream));
-    SGW_CK(cudaStreamSynchronize(op->stream));
+    if ((s = read_count(op, nactive, &h_active)) != SGW_OK) return s;
     if (!pick || h_active == 0) {
       if (pick) {  // every shift converged before the round limit: the final pass writes the estimates
         rf_select<T><<<R, tb, 0, op->stream>>>(R, S, n, npwx, st.r64, rround, scale, st.bnorm, st.Z, seed, perm,
