@@ -622,8 +622,8 @@ def run_gpu(args, rank, world):
     from sternheimergw_gb300 import linter
     nocc = s["nocc"]
 
-    # end to end through the C ABI with page-locked host buffers from sgw_host_alloc
-    # (transparent huge pages): the mixed path (headline) and the plain FP64 drop-in,
+    # end to end through the C ABI with page-locked host buffers from sgw_host_alloc:
+    # the mixed path (headline) and the plain FP64 drop-in,
     # right after the device-resident steps; solves/s follow once the converged
     # fractions are known.
     bb_h = sg.host_array(bb.shape)
@@ -818,7 +818,7 @@ def run_gpu(args, rank, world):
             "e2e": {"value": e2e["mixed"]["value"], "unit": "solves/s", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e["mixed"]["ms"],
                     "ms_per_step_all": e2e["mixed"]["all"], "pairs_per_s": e2e["mixed"]["pairs_per_s"],
-                    "host_buffers": "sgw_host_alloc (page-locked, transparent huge pages)",
+                    "host_buffers": "sgw_host_alloc (page-locked base pages, populated before pinning)",
                     "output_huge_page_fraction": None if x_huge is None else x_huge / x_h.nbytes,
                     "host_link_plain_copy": link,
                     "host_link_at_start": link_start,

@@ -516,12 +516,12 @@ sgw_status sgw_operator_autotune(sgw_operator* op, int32_t precision, sgw_tune_r
 /* Page-locked host buffer for the host-memory form of the calls (memory = 0),
  * no counterpart in the reference (its arrays are Fortran allocatables; a
  * Fortran caller maps the pointer with c_f_pointer).  The buffer is an
- * anonymous mapping aligned to the transparent-huge-page size and advised
- * MADV_HUGEPAGE, populated with a non-zero pattern, registered with
- * cudaHostRegister and then zero-filled.  Copies into cudaHostAlloc memory, and
- * into mappings populated with zeros before they were registered, ran at
- * 3-56 GB/s on the GB300 hosts measured (from the start or after a large
- * solve); into this buffer at 193 GB/s out and 211 GB/s in throughout.
+ * anonymous mapping on base pages (MADV_NOHUGEPAGE), populated with a non-zero
+ * pattern, registered with cudaHostRegister and then zero-filled.  Copies into
+ * cudaHostAlloc memory, into mappings on transparent huge pages and into
+ * mappings populated with zeros before they were registered ran at 3-56 GB/s
+ * on the GB300 hosts measured (from the start, or once large solves had run);
+ * into this buffer at 193 GB/s out and 211 GB/s in throughout.
  * bytes = 0 returns *ptr = NULL.  sgw_host_free takes only pointers
  * returned by sgw_host_alloc (NULL is a no-op). */
 sgw_status sgw_host_alloc(size_t bytes, void** ptr);

@@ -694,22 +694,10 @@ static sgw_status apply_ex(sgw_operator* op, int precision, int memory, sgw_zcom
 }
 
 // ---------------------------------------------------------------------------
-// Page-locked host buffers on transparent huge pages
+// Page-locked host buffers
 // ---------------------------------------------------------------------------
 static std::mutex g_host_mu;
 static std::unordered_map<void*, size_t> g_host_bufs;  // start -> mapped length
-
-// PMD (huge page) size of the running kernel: 2 MiB with 4 KiB base pages,
-// 512 MiB with 64 KiB base pages.
-static size_t thp_size() {
-  size_t v = 0;
-  if (FILE* f = std::fopen("/sys/kernel/mm/transparent_hugepage/hpage_pmd_size", "r")) {
-    unsigned long long u = 0;
-    if (std::fscanf(f, "%llu", &u) == 1) v = (size_t)u;
-    std::fclose(f);
-  }
-  return (v == 0 || (v & (v - 1))) ? ((size_t)2 << 20) : v;
-}
 
 static sgw_status host_alloc(size_t bytes, void** ptr) {
   if (!ptr) return arg_error("null pointer argument");
@@ -718,29 +706,18 @@ static sgw_status host_alloc(size_t bytes, void** ptr) {
   if (bytes > ((size_t)1 << 62)) return arg_error("sgw_host_alloc: size out of range");
   const size_t page = (size_t)sysconf(_SC_PAGESIZE);
   const size_t len = (bytes + page - 1) / page * page;
-  const size_t huge = thp_size();
-  // a huge page backs only a huge-page-aligned range: map one huge page more
-  // than needed and cut the unaligned head and the tail off
-  const size_t slack = len >= huge ? huge : 0;
-  void* raw = mmap(nullptr, len + slack, PROT_READ | PROT_WRITE, MAP_PRIVATE | MAP_ANONYMOUS, -1, 0);
+  void* raw = mmap(nullptr, len, PROT_READ | PROT_WRITE, MAP_PRIVATE | MAP_ANONYMOUS, -1, 0);
   if (raw == MAP_FAILED) {
     set_error("mmap of " + std::to_string(len) + " bytes failed");
     return SGW_ERR_NOMEM;
   }
   char* p = static_cast<char*>(raw);
-  if (slack) {
-    const uintptr_t a = ((uintptr_t)raw + huge - 1) & ~(uintptr_t)(huge - 1);
-    const size_t head = a - (uintptr_t)raw;
-    if (head) munmap(raw, head);
-    if (slack - head) munmap(reinterpret_cast<char*>(a) + len, slack - head);
-    p = reinterpret_cast<char*>(a);
-  }
-  madvise(p, len, MADV_HUGEPAGE);  // advisory: base pages remain if THP is off
-  // Populate with a non-zero pattern, pin, then zero.  Buffers populated with
-  // zeros before cudaHostRegister were measured to copy at 3-18 GB/s on these
-  // hosts (from the start, or after a while), on huge and on base pages alike,
-  // while the same buffers populated with a non-zero pattern copied at 193 GB/s
-  // out and 211 GB/s in throughout - also after host work and large solves.
+  // Base pages, populated with a non-zero pattern, pinned, then zeroed.  On
+  // the GB300 hosts measured, 4.6 GB buffers on transparent huge pages, and
+  // buffers populated with zeros before cudaHostRegister, copied at 3-36 GB/s
+  // out once large solves had run (cudaHostAlloc memory at 6-18 GB/s); this
+  // form copied at 193 GB/s out and 211 GB/s in at every checkpoint.
+  madvise(p, len, MADV_NOHUGEPAGE);
   std::memset(p, 0x5a, len);
   const cudaError_t e = cudaHostRegister(p, len, cudaHostRegisterPortable);
   if (e != cudaSuccess) {

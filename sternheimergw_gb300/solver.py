@@ -249,9 +249,9 @@ def _order_after_torch(AA: _Operator):
 
 
 def host_array(shape, dtype=np.complex128):
-    """Zero-filled numpy array in page-locked host memory on transparent huge
-    pages (sgw_host_alloc), for the host-memory form of the calls: result
-    copies into it keep the full device-to-host bandwidth after a large solve.
+    """Zero-filled numpy array in page-locked host memory (sgw_host_alloc), for
+    the host-memory form of the calls: result copies into it keep the full
+    device-to-host bandwidth after a large solve.
     The memory is unpinned and unmapped when the array and every view of it
     are gone."""
     import weakref
