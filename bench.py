@@ -47,7 +47,7 @@ METRIC = "Sternheimer solves/sec: batched mixed vs plain FP64, same GPU, W err â
 # on 152 right-hand sides of this workload (dram__bytes_read.sum +
 # dram__bytes_write.sum over the same count's algorithmic bytes); roofline.traffic
 # is this ratio times the algorithmic bytes of the timed launches.
-NCU_TRAFFIC_OVER_ALGORITHMIC = {"fp32": 2.87, "fp64": 14.0}
+NCU_TRAFFIC_OVER_ALGORITHMIC = {"fp32": 2.67, "fp64": 14.0}
 CONV_TOL = 1e-6          # a pair is a solve when its true relative residual is at most this
 CONV_SAMPLE = 32         # right-hand sides of the convergence sample (all 70 shifts each)
 WORKLOAD = "sc8 a=10.26 25Ry 40^3 npw=2293 nkb=32 nocc=16 npert=113 nfreq=35 (S=70) lmax=4 thr=1e-10"
