@@ -26,6 +26,7 @@ Run ``python bench.py`` (1 GPU) or under torchrun for N replicas (weak scaling).
 from __future__ import annotations
 
 import argparse
+import contextlib
 import json
 import math
 import os
@@ -595,16 +596,66 @@ def run_gpu(args, rank, world):
         if world > 1:
             dist.barrier()
 
+    # clocks and throttle reasons are sampled over both timed regions (end to end, then
+    # device-resident)
+    clk_stack = contextlib.ExitStack()
+    clk = clk_stack.enter_context(ClockSampler(dev))
+    # end to end through the C ABI with page-locked host buffers from sgw_host_alloc:
+    # the mixed path (headline) and the plain FP64 drop-in, before the device-resident
+    # steps; solves/s follow once the converged fractions are known.
+    e2e = link = link_fresh = x_h = x_huge = None
+    if not args.no_extras and args.precision == "both":
+        bb_h = sg.host_array(bb.shape)
+        bb_h[...] = bb
+        sg_h = sg.host_array(sigma.shape)
+        sg_h[...] = sigma
+        x_h = sg.host_array((nrhs, S, n))
+        x_huge = huge_page_bytes(x_h.ctypes.data, x_h.nbytes)
+
+        def plain_link(xs):
+            """One plain copy of the 4.6 GB each way between a device array and x_h (CUDA events)."""
+            out = {}
+            xt = torch.from_numpy(x_h)
+            for name, dst, src in (("d2h_gbs", xt, xs), ("h2d_gbs", xs, xt)):
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                torch.cuda.synchronize()
+                e0.record()
+                dst.copy_(src, non_blocking=True)
+                e1.record()
+                e1.synchronize()
+                out[name] = x_h.nbytes / (e0.elapsed_time(e1) * 1e-3) / 1e9
+            return out
+
+        xs = torch.empty_like(xm_d)
+        link_fresh = plain_link(xs)
+        # untimed calls first: they allocate the library's host-path staging buffers
+        for prec in (1, 0):
+            sg.solve_batch(op, bb_h, sg_h, lmax=LMAX, threshold=THRESHOLD, precision=prec, out=x_h)
+        # the host link alone, just before the timed calls
+        link = plain_link(xs)
+        del xs
+        e2e = {}
+        for prec, key in ((1, "mixed"), (0, "fp64")):
+            e2e_ms, copy_ms = [], []
+            for k in range(max(1, min(args.steps, 3))):
+                flush_l2(l2)
+                torch.cuda.synchronize()
+                t = time.time()
+                sg.solve_batch(op, bb_h, sg_h, lmax=LMAX, threshold=THRESHOLD, precision=prec, out=x_h)
+                e2e_ms.append((time.time() - t) * 1e3)
+                copy_ms.append((op.kernel_timing(6)[0], op.kernel_timing(7)[0]))
+            med = float(np.median(e2e_ms))
+            e2e[key] = dict(ms=med, all=[float(v) for v in e2e_ms], copies=copy_ms, pairs_per_s=world * nrhs * S / (med * 1e-3))
     barrier()
-    with ClockSampler(dev) as clk:
-        t0 = time.time()
-        p64 = pm = None
-        if args.precision in ("both", "fp64"):
-            p64 = time_path(op, bb_d, sg_d, x64_d, 0, args.warmup, args.steps, l2, "fp64")
-        if args.precision in ("both", "mixed"):
-            pm = time_path(op, bb_d, sg_d, xm_d, 1, args.warmup, args.steps, l2, "mixed")
-        barrier()
-        wall = time.time() - t0
+    t0 = time.time()
+    p64 = pm = None
+    if args.precision in ("both", "fp64"):
+        p64 = time_path(op, bb_d, sg_d, x64_d, 0, args.warmup, args.steps, l2, "fp64")
+    if args.precision in ("both", "mixed"):
+        pm = time_path(op, bb_d, sg_d, xm_d, 1, args.warmup, args.steps, l2, "mixed")
+    barrier()
+    wall = time.time() - t0
+    clk_stack.close()
     if args.no_extras or p64 is None or pm is None:
         out = None
         if rank == 0:
@@ -622,45 +673,6 @@ def run_gpu(args, rank, world):
     from sternheimergw_gb300 import linter
     nocc = s["nocc"]
 
-    # end to end through the C ABI with page-locked host buffers from sgw_host_alloc:
-    # the mixed path (headline) and the plain FP64 drop-in,
-    # right after the device-resident steps; solves/s follow once the converged
-    # fractions are known.
-    bb_h = sg.host_array(bb.shape)
-    bb_h[...] = bb
-    sg_h = sg.host_array(sigma.shape)
-    sg_h[...] = sigma
-    x_h = sg.host_array((nrhs, S, n))
-    x_huge = huge_page_bytes(x_h.ctypes.data, x_h.nbytes)
-    # untimed calls first: they allocate the library's host-path staging buffers
-    for prec in (1, 0):
-        sg.solve_batch(op, bb_h, sg_h, lmax=LMAX, threshold=THRESHOLD, precision=prec, out=x_h)
-    # the host link alone: one plain copy of the same 4.6 GB each way between the
-    # device solution and the output buffer (CUDA events, current stream)
-    link = {}
-    xt = torch.from_numpy(x_h)
-    xs = torch.empty_like(xm_d)
-    for name, dst, src in (("d2h_gbs", xt, xs), ("h2d_gbs", xs, xt)):
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        torch.cuda.synchronize()
-        e0.record()
-        dst.copy_(src, non_blocking=True)
-        e1.record()
-        e1.synchronize()
-        link[name] = x_h.nbytes / (e0.elapsed_time(e1) * 1e-3) / 1e9
-    del xt, xs
-    e2e = {}
-    for prec, key in ((1, "mixed"), (0, "fp64")):
-        e2e_ms, copy_ms = [], []
-        for k in range(max(1, min(args.steps, 3))):
-            flush_l2(l2)
-            torch.cuda.synchronize()
-            t = time.time()
-            sg.solve_batch(op, bb_h, sg_h, lmax=LMAX, threshold=THRESHOLD, precision=prec, out=x_h)
-            e2e_ms.append((time.time() - t) * 1e3)
-            copy_ms.append((op.kernel_timing(6)[0], op.kernel_timing(7)[0]))
-        med = float(np.median(e2e_ms))
-        e2e[key] = dict(ms=med, all=[float(v) for v in e2e_ms], copies=copy_ms, pairs_per_s=world * pairs / (med * 1e-3))
     # --- the checker: true residuals of a fixed sample with the oracle's apply ---------------
     rows = sample_rows(nrhs)
     res64 = true_residuals(s, bb, sigma, x64_d, rows)
@@ -821,6 +833,7 @@ def run_gpu(args, rank, world):
                     "host_buffers": "sgw_host_alloc (page-locked base pages, populated before pinning)",
                     "output_huge_page_fraction": None if x_huge is None else x_huge / x_h.nbytes,
                     "host_link_plain_copy": link,
+                    "host_link_fresh_buffer": link_fresh,
                     "host_link_at_start": link_start,
                     "copy_in_ms_all": [c[0] for c in e2e["mixed"]["copies"]],
                     "copy_out_ms_all": [c[1] for c in e2e["mixed"]["copies"]]},
