@@ -131,6 +131,21 @@ static sgw_status init_common(sgw_operator* op) {
   for (int i = 0; i < 2 * kMaxTimedLaunches; ++i) SGW_CK(cudaEventCreate(&op->kev[i]));
   SGW_CK(cudaHostAlloc(reinterpret_cast<void**>(&op->h_count), sizeof(int), cudaHostAllocMapped));
   SGW_CK(cudaHostGetDevicePointer(reinterpret_cast<void**>(&op->d_count_alias), op->h_count, 0));
+  return host_staging(op, (size_t)1 << 20, nullptr);
+}
+
+sgw_status host_staging(sgw_operator* op, size_t bytes, void** out) {
+  if (bytes > op->h_small_bytes) {
+    if (op->h_small) {
+      SGW_CK(cudaStreamSynchronize(op->stream));
+      cudaFreeHost(op->h_small);
+      op->h_small = nullptr;
+      op->h_small_bytes = 0;
+    }
+    SGW_CK(cudaHostAlloc(&op->h_small, bytes, cudaHostAllocDefault));
+    op->h_small_bytes = bytes;
+  }
+  if (out) *out = op->h_small;
   return SGW_OK;
 }
 
@@ -507,9 +522,13 @@ static sgw_status solve_batch(sgw_operator* op, const sgw_batch_desc* d, const s
       if (resid_user && (s = op->st_resid.ensure(sizeof(double) * (size_t)R * S)) != SGW_OK) return s;
       bo.resid = resid_user ? op->st_resid.as<double>() : nullptr;
       s = solve_batch_opts(op, b, d->precision, d->refine_max, d->refine_threshold, bo);
-      if (s == SGW_OK && resid_user)
-        SGW_CK(cudaMemcpyAsync(resid_user, op->st_resid.p, sizeof(double) * (size_t)R * S, cudaMemcpyDeviceToHost,
-                               op->stream));
+      if (s == SGW_OK && resid_user) {  // through the page-locked staging, after ierr and iters
+        void* hs = nullptr;
+        if ((s = host_staging(op, 2 * sizeof(int) * (size_t)R + sizeof(double) * (size_t)R * S, &hs)) != SGW_OK)
+          return s;
+        SGW_CK(cudaMemcpyAsync(static_cast<char*>(hs) + 2 * sizeof(int) * (size_t)R, op->st_resid.p,
+                               sizeof(double) * (size_t)R * S, cudaMemcpyDeviceToHost, op->stream));
+      }
     } else {
       s = solve_batch_device(op, b, d->precision, d->refine_max, d->refine_threshold, packed ? &oc : nullptr);
     }
@@ -532,11 +551,20 @@ static sgw_status solve_batch(sgw_operator* op, const sgw_batch_desc* d, const s
                                  op->st_xx.as<zcd>() + (size_t)r * S * n, sizeof(zcd) * n, sizeof(zcd) * n, S,
                                  cudaMemcpyDeviceToHost, op->stream));
     }
-    SGW_CK(cudaMemcpyAsync(d->ierr, op->st_ierr.p, sizeof(int) * R, cudaMemcpyDeviceToHost, op->stream));
-    if (d->iters) SGW_CK(cudaMemcpyAsync(d->iters, op->st_iters.p, sizeof(int) * R, cudaMemcpyDeviceToHost, op->stream));
+    // ierr and iters through the page-locked staging (they may be pageable arrays)
+    void* hs = nullptr;
+    const size_t resid_bytes = (extended && resid_user) ? sizeof(double) * (size_t)R * S : 0;
+    if ((s = host_staging(op, 2 * sizeof(int) * (size_t)R + resid_bytes, &hs)) != SGW_OK) return s;
+    int* hs_ierr = static_cast<int*>(hs);
+    SGW_CK(cudaMemcpyAsync(hs_ierr, op->st_ierr.p, sizeof(int) * R, cudaMemcpyDeviceToHost, op->stream));
+    if (d->iters)
+      SGW_CK(cudaMemcpyAsync(hs_ierr + R, op->st_iters.p, sizeof(int) * R, cudaMemcpyDeviceToHost, op->stream));
     ktime_end(op, tout);
     SGW_CK(cudaEventRecord(op->ev1, op->stream));
     SGW_CK(cudaStreamSynchronize(op->stream));
+    std::memcpy(d->ierr, hs_ierr, sizeof(int) * R);
+    if (d->iters) std::memcpy(d->iters, hs_ierr + R, sizeof(int) * R);
+    if (resid_bytes) std::memcpy(resid_user, hs_ierr + 2 * R, resid_bytes);
   }
   float ms = 0.f;
   SGW_CK(cudaEventElapsedTime(&ms, op->ev0, op->ev1));
@@ -805,6 +833,7 @@ sgw_status sgw_operator_destroy(sgw_operator* op) {
   if (op->copy_stream) cudaStreamDestroy(op->copy_stream);
   if (op->stream) cudaStreamDestroy(op->stream);
   if (op->h_count) cudaFreeHost(op->h_count);
+  if (op->h_small) cudaFreeHost(op->h_small);
   delete op;
   return SGW_OK;
 }

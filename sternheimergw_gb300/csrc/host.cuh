@@ -124,6 +124,11 @@ struct sgw_operator {
   // page-locked, device-mapped host ints: counts read back between rounds (read_count)
   int* h_count = nullptr;
   int* d_count_alias = nullptr;
+  // page-locked staging of the small per-call outputs of the host-memory form
+  // (ierr, iters, residual estimates): copied to the caller's arrays after the
+  // stream is synchronised (host_staging)
+  void* h_small = nullptr;
+  size_t h_small_bytes = 0;
   cudaEvent_t lev0 = nullptr, lev1 = nullptr;  // sgw_coulomb_rhs / sgw_chi timing
   double last_ms = 0.0;
   long long last_launches = 0;
@@ -214,6 +219,11 @@ void collect_kernel_times(sgw_operator* op);
 // the stream is synchronised.  No copy engine is involved, so the read does not
 // queue behind a large result copy in flight on the copy stream.
 sgw_status read_count(sgw_operator* op, const int* dev, int* out);
+// The operator's page-locked staging for small device-to-host results, at
+// least `bytes` long.  Device-to-host copies into pageable memory were measured
+// to slow later copies into registered buffers (such as sgw_host_alloc's) to
+// 6-8 GB/s; small results therefore land here and are copied on the host.
+sgw_status host_staging(sgw_operator* op, size_t bytes, void** out);
 // `stream` waits for the work queued so far on `caller` (event `ev` is reused).
 sgw_status order_after(cudaStream_t stream, cudaStream_t caller, cudaEvent_t ev);
 

@@ -92,8 +92,10 @@ static sgw_status coulomb_rhs(sgw_operator* op, const sgw_rhs_desc* d) {
                              (size_t)d->npert * nocc, cudaMemcpyDeviceToHost, op->stream));
   SGW_CK(cudaEventRecord(op->lev1, op->stream));
   int bad = 0;
-  SGW_CK(cudaMemcpyAsync(&bad, a.bad_index, sizeof(int), cudaMemcpyDeviceToHost, op->stream));
-  SGW_CK(cudaStreamSynchronize(op->stream));
+  {
+    const sgw_status sc = read_count(op, a.bad_index, &bad);
+    if (sc != SGW_OK) return sc;
+  }
   float ms = 0.f;
   SGW_CK(cudaEventElapsedTime(&ms, op->lev0, op->lev1));
   op->kernel_ms[K_RHS] = ms;
@@ -518,8 +520,10 @@ static sgw_status vjp(sgw_operator* op, const sgw_vjp_desc* d) {
   }
   SGW_CK(cudaEventRecord(op->lev1, op->stream));
   int bad = 0;
-  SGW_CK(cudaMemcpyAsync(&bad, ra.bad_index, sizeof(int), cudaMemcpyDeviceToHost, op->stream));
-  SGW_CK(cudaStreamSynchronize(op->stream));
+  {
+    const sgw_status sc = read_count(op, ra.bad_index, &bad);
+    if (sc != SGW_OK) return sc;
+  }
   float ms = 0.f;
   SGW_CK(cudaEventElapsedTime(&ms, op->lev0, op->lev1));
   op->kernel_ms[K_VJP] = ms;

@@ -221,9 +221,11 @@ sgw_status screened_coulomb(sgw_operator* op, const sgw_w_desc* d) {
     if (d->w) SGW_CK(cudaMemcpyAsync(d->w, w_d, sizeof(zcd) * F * PP, cudaMemcpyDeviceToHost, op->stream));
   }
   int sing = 0;
-  SGW_CK(cudaMemcpyAsync(&sing, flag, sizeof(int), cudaMemcpyDeviceToHost, op->stream));
   SGW_CK(cudaEventRecord(op->lev1, op->stream));
-  SGW_CK(cudaStreamSynchronize(op->stream));
+  {
+    const sgw_status sc = read_count(op, flag, &sing);
+    if (sc != SGW_OK) return sc;
+  }
   float ms = 0.f;
   SGW_CK(cudaEventElapsedTime(&ms, op->lev0, op->lev1));
   op->kernel_ms[K_SCREEN] = ms;
