@@ -129,8 +129,6 @@ static sgw_status init_common(sgw_operator* op) {
   SGW_CK(cudaEventCreate(&op->lev0));
   SGW_CK(cudaEventCreate(&op->lev1));
   for (int i = 0; i < 2 * kMaxTimedLaunches; ++i) SGW_CK(cudaEventCreate(&op->kev[i]));
-  SGW_CK(cudaHostAlloc(reinterpret_cast<void**>(&op->h_count), sizeof(int), cudaHostAllocMapped));
-  SGW_CK(cudaHostGetDevicePointer(reinterpret_cast<void**>(&op->d_count_alias), op->h_count, 0));
   return host_staging(op, (size_t)1 << 20, nullptr);
 }
 
@@ -149,18 +147,13 @@ sgw_status host_staging(sgw_operator* op, size_t bytes, void** out) {
   return SGW_OK;
 }
 
-static __global__ void publish_count(const int* src, int* dst) {
-  *reinterpret_cast<volatile int*>(dst) = *src;
-  __threadfence_system();
-}
-
 sgw_status read_count(sgw_operator* op, const int* dev, int* out) {
-  *reinterpret_cast<volatile int*>(op->h_count) = -1;
-  publish_count<<<1, 1, 0, op->stream>>>(dev, op->d_count_alias);
-  SGW_CK(cudaGetLastError());
-  op->last_launches += 1;
+  void* hs = nullptr;
+  const sgw_status s = host_staging(op, sizeof(int), &hs);
+  if (s != SGW_OK) return s;
+  SGW_CK(cudaMemcpyAsync(hs, dev, sizeof(int), cudaMemcpyDeviceToHost, op->stream));
   SGW_CK(cudaStreamSynchronize(op->stream));
-  *out = *reinterpret_cast<volatile int*>(op->h_count);
+  std::memcpy(out, hs, sizeof(int));
   return SGW_OK;
 }
 
@@ -832,7 +825,6 @@ sgw_status sgw_operator_destroy(sgw_operator* op) {
   if (op->ev_caller) cudaEventDestroy(op->ev_caller);
   if (op->copy_stream) cudaStreamDestroy(op->copy_stream);
   if (op->stream) cudaStreamDestroy(op->stream);
-  if (op->h_count) cudaFreeHost(op->h_count);
   if (op->h_small) cudaFreeHost(op->h_small);
   delete op;
   return SGW_OK;

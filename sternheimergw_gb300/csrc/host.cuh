@@ -121,9 +121,6 @@ struct sgw_operator {
   cudaStream_t copy_stream = nullptr;                 // host-path result copies overlapped with the solve
   cudaEvent_t ev_acc = nullptr, ev_copied = nullptr;  // its hand-offs (no timing)
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-  // page-locked, device-mapped host ints: counts read back between rounds (read_count)
-  int* h_count = nullptr;
-  int* d_count_alias = nullptr;
   // page-locked staging of the small per-call outputs of the host-memory form
   // (ierr, iters, residual estimates): copied to the caller's arrays after the
   // stream is synchronised (host_staging)
@@ -214,10 +211,8 @@ class CallScope {
 // Sum the per-kernel event pairs of the last call into kernel_ms / kernel_launches
 // (the handle's stream must be synchronised).
 void collect_kernel_times(sgw_operator* op);
-// A device int, read on the host after the work queued on op->stream: one
-// thread stores it into the operator's page-locked, device-mapped host int and
-// the stream is synchronised.  No copy engine is involved, so the read does not
-// queue behind a large result copy in flight on the copy stream.
+// A device int, read on the host after the work queued on op->stream, through
+// the operator's page-locked staging (host_staging).
 sgw_status read_count(sgw_operator* op, const int* dev, int* out);
 // The operator's page-locked staging for small device-to-host results, at
 // least `bytes` long.  Device-to-host copies into pageable memory were measured
