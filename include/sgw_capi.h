@@ -521,10 +521,10 @@ sgw_status sgw_operator_autotune(sgw_operator* op, int32_t precision, sgw_tune_r
  * cudaHostAlloc memory, into mappings on transparent huge pages and into
  * mappings populated with zeros before they were registered ran at 3-56 GB/s
  * on the GB300 hosts measured (from the start, or once large solves had run);
- * into this buffer at 193 GB/s out and 211 GB/s in.  Any registered buffer
- * slowed to 6-8 GB/s after a call that made the library allocate large device
- * workspaces (the first solve of a handle in a precision): allocate result
- * buffers after that call.  bytes = 0 returns *ptr = NULL.  sgw_host_free takes only pointers
+ * into this buffer at 193 GB/s out and 211 GB/s in.  In one probe a registered
+ * buffer slowed to 6-8 GB/s after a call that made the library allocate large
+ * device workspaces (the first solve of a handle in a precision), so result
+ * buffers are best allocated after that call.  bytes = 0 returns *ptr = NULL.  sgw_host_free takes only pointers
  * returned by sgw_host_alloc (NULL is a no-op). */
 sgw_status sgw_host_alloc(size_t bytes, void** ptr);
 sgw_status sgw_host_free(void* ptr);
